@@ -1,0 +1,244 @@
+/*
+ * synchrad_gb300: C ABI of the GB300 (sm_103a) radiation-integral library.
+ *
+ * The library evaluates SynchRad's far-field (Lienard-Wiechert spectral sum
+ * over track steps, per (omega, theta, phi) point) and near-field (screen at a
+ * finite distance) integrals on the GPU.  All pointers named "device" are CUDA
+ * device pointers owned by the caller; nothing here allocates device memory.
+ * Every entry point is stream-ordered on `stream` (a cudaStream_t, NULL for the
+ * legacy default stream), returns SR_OK or a negative SR_ERR_* code, and leaves
+ * a message for sr_last_error() on failure.  Output spectra are accumulated in
+ * place (+=), as the reference kernels do.
+ *
+ * Spectrum layout on the device (the reference's, synchrad/calc.py:455-456):
+ *   out[k][iPhi][iTheta|iR][iOmega],  k < n_snaps,
+ * i.e. point index gti = iOmega + nOmega*(iTheta + nTheta*iPhi).
+ */
+#ifndef SYNCHRAD_GB300_H
+#define SYNCHRAD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  SR_OK = 0,
+  SR_ERR_INVALID = -1,     /* bad argument (null pointer, size, combination) */
+  SR_ERR_UNSUPPORTED = -2, /* valid but not implemented for this mode/comp */
+  SR_ERR_CUDA = -3,        /* a CUDA launch or runtime call failed */
+  SR_ERR_WORKSPACE = -4,   /* workspace missing or smaller than required */
+  SR_ERR_TIMEOUT = -5      /* a kernel wait ran out of time (see sr_workspace_status) */
+};
+
+enum { SR_DTYPE_F64 = 0, SR_DTYPE_F32 = 1 };
+enum { SR_MODE_FAR = 0, SR_MODE_NEAR = 1 };
+
+/* `comp` of calculate_spectrum (synchrad/calc.py:133-144, 458-465). */
+enum {
+  SR_COMP_TOTAL = 0,             /* 1 output:  sum_tracks w dt^2 |A|^2 */
+  SR_COMP_CARTESIAN = 1,         /* 3 outputs: |A_x|^2, |A_y|^2, |A_z|^2 */
+  SR_COMP_CARTESIAN_COMPLEX = 2, /* 6 outputs: sqrt(w) dt Re/Im A_{x,y,z} */
+  SR_COMP_SPHERIC = 3,           /* 3 outputs: |A_r|^2, |A_theta|^2, |A_phi|^2 (far) */
+  SR_COMP_SPHERIC_COMPLEX = 4    /* 6 outputs: sqrt(w) dt Re/Im A_{r,theta,phi} (far) */
+};
+
+/* Arithmetic of one evaluation. */
+enum {
+  SR_PREC_DOUBLE = 0,       /* FP64 throughout: the plain port of the reference kernel */
+  SR_PREC_FLOAT = 1,        /* FP32 throughout: the reference's dtype='float' */
+  SR_PREC_FLOAT_NATIVE = 2, /* FP32 with fast intrinsics: dtype='float' + 'native' */
+  SR_PREC_MIXED = 3         /* FP32 bulk, double-float phase, compensated sums, FP64 spectrum */
+};
+
+/*
+ * A batch of tracks in CSR form.  Track t owns steps offsets[t] .. offsets[t+1]-1
+ * of the concatenated arrays x..uz.  Per-track values mirror one reference
+ * kernel launch (synchrad/calc.py:306-322): wp = weight[t], itStart =
+ * it_start[t], itEnd = it_end[t], nSteps = offsets[t+1]-offsets[t], and the
+ * snapshot iterations row snap_its[t*snap_stride .. + n_snaps) (snap_stride 0:
+ * one row shared by every track, the it_range case).
+ */
+typedef struct sr_tracks {
+  uint32_t n_tracks;
+  uint32_t dtype;           /* SR_DTYPE_F64 | SR_DTYPE_F32: element type of x..uz */
+  int64_t total_steps;      /* host copy of offsets[n_tracks] */
+  const int64_t *offsets;   /* device [n_tracks + 1], offsets[0] == 0 */
+  const void *x, *y, *z;    /* device [total_steps] positions (c = 1 units) */
+  const void *ux, *uy, *uz; /* device [total_steps] momenta gamma*beta */
+  const double *weight;     /* device [n_tracks] */
+  const uint32_t *it_start; /* device [n_tracks] */
+  const uint32_t *it_end;   /* device [n_tracks] */
+  const uint32_t *snap_its; /* device, see above */
+  uint32_t snap_stride;
+  uint32_t n_snaps;
+  double dt;                /* c*dt, the reference's timeStep */
+} sr_tracks;
+
+/*
+ * The spectral grid as the reference uploads it (synchrad/calc.py:486-512):
+ * omega already multiplied by 2*pi; far field: sinTheta, cosTheta, sinPhi,
+ * cosPhi; near field: radius, sinPhi, cosPhi and the screen distance.
+ */
+typedef struct sr_grid {
+  uint32_t mode;            /* SR_MODE_FAR | SR_MODE_NEAR */
+  uint32_t dtype;           /* element type of the axis arrays */
+  uint32_t n_omega;
+  uint32_t n_theta;         /* n_R in near mode */
+  uint32_t n_phi;
+  uint32_t reserved;
+  const void *omega;        /* device [n_omega] */
+  const void *axis1;        /* device: far sinTheta [n_theta], near radius [n_R] */
+  const void *axis2;        /* device: far cosTheta [n_theta], near unused */
+  const void *sin_phi;      /* device [n_phi] */
+  const void *cos_phi;      /* device [n_phi] */
+  const void *form_factor;  /* device [n_omega]; used by far cartesian_complex only */
+  double L_screen;          /* near mode: distance to the screen */
+} sr_grid;
+
+/* ---------------------------------------------------------------------------
+ * Batched evaluation: the GB300-native entry point.
+ *
+ * Replaces the per-track loop of SynchRad.calculate_spectrum
+ * (synchrad/calc.py:257-267) and the kernel launches it makes
+ * (synchrad/calc.py:324-353): one call evaluates every track of the batch and
+ * accumulates the incoherent (or coherent, for *_complex) sum into `out`.
+ *   out:  n_out device arrays (1, 3 or 6 by comp), element type double for
+ *         SR_PREC_DOUBLE / SR_PREC_MIXED and float for SR_PREC_FLOAT*.
+ *   workspace: device scratch of at least sr_workspace_bytes(...) bytes,
+ *         256-byte aligned (NULL allowed when that size is 0).
+ * Track and grid element types: SR_PREC_DOUBLE needs F64 tracks and grid,
+ * SR_PREC_FLOAT* need F32 tracks and grid, SR_PREC_MIXED takes F64 or F32
+ * tracks with an F64 grid.
+ * ------------------------------------------------------------------------- */
+int sr_spectrum(const sr_tracks *tracks, const sr_grid *grid, int comp,
+                int precision, void *const *out, void *workspace,
+                size_t workspace_bytes, void *stream);
+
+/* Scratch bytes sr_spectrum needs for these sizes (reads host fields only). */
+int64_t sr_workspace_bytes(const sr_tracks *tracks, const sr_grid *grid,
+                           int comp, int precision);
+
+/* Synchronises `stream` and reads the kernels' status word from a workspace
+ * used by sr_spectrum: SR_OK, or SR_ERR_TIMEOUT if a bounded wait expired. */
+int sr_workspace_status(const void *workspace, void *stream);
+
+/* Message of the last failure on the calling thread ("" if none). */
+const char *sr_last_error(void);
+
+/* Library version, major*10000 + minor*100 + patch. */
+int sr_version(void);
+
+/* ---------------------------------------------------------------------------
+ * Per-track entry points: the reference's OpenCL kernels, one launch each.
+ *
+ * Same argument order and meaning as the kernels in
+ * synchrad/kernel_farfield.cl and synchrad/kernel_nearfield.cl as
+ * synchrad/calc.py:306-353 binds them, with `dtype` (SR_DTYPE_F64 or
+ * SR_DTYPE_F32, the Mako ${my_dtype}) as the first argument and the stream as
+ * the last.  Every array argument has element type `dtype`; `native` selects
+ * the ${f_native} intrinsics for SR_DTYPE_F32.  No workspace is needed.
+ * ------------------------------------------------------------------------- */
+
+/* synchrad/kernel_farfield.cl:6-28 `total` */
+int sr_far_total(int dtype, int native, void *spectrum, const void *x,
+                 const void *y, const void *z, const void *ux, const void *uy,
+                 const void *uz, double wp, uint32_t itStart, uint32_t itEnd,
+                 uint32_t nSteps, const void *omega, const void *sinTheta,
+                 const void *cosTheta, const void *sinPhi, const void *cosPhi,
+                 uint32_t nOmega, uint32_t nTheta, uint32_t nPhi, double dt,
+                 uint32_t nSnaps, const uint32_t *itSnaps, void *stream);
+
+/* synchrad/kernel_farfield.cl:111-135 `cartesian_comps` */
+int sr_far_cartesian_comps(int dtype, int native, void *spectrum1,
+                           void *spectrum2, void *spectrum3, const void *x,
+                           const void *y, const void *z, const void *ux,
+                           const void *uy, const void *uz, double wp,
+                           uint32_t itStart, uint32_t itEnd, uint32_t nSteps,
+                           const void *omega, const void *sinTheta,
+                           const void *cosTheta, const void *sinPhi,
+                           const void *cosPhi, uint32_t nOmega,
+                           uint32_t nTheta, uint32_t nPhi, double dt,
+                           uint32_t nSnaps, const uint32_t *itSnaps,
+                           void *stream);
+
+/* synchrad/kernel_farfield.cl:227-255 `cartesian_comps_complex` */
+int sr_far_cartesian_comps_complex(
+    int dtype, int native, void *spectrum1_re, void *spectrum1_im,
+    void *spectrum2_re, void *spectrum2_im, void *spectrum3_re,
+    void *spectrum3_im, const void *x, const void *y, const void *z,
+    const void *ux, const void *uy, const void *uz, double wp,
+    uint32_t itStart, uint32_t itEnd, uint32_t nSteps, const void *omega,
+    const void *sinTheta, const void *cosTheta, const void *sinPhi,
+    const void *cosPhi, uint32_t nOmega, uint32_t nTheta, uint32_t nPhi,
+    double dt, uint32_t nSnaps, const uint32_t *itSnaps,
+    const void *FormFactor, void *stream);
+
+/* synchrad/kernel_farfield.cl:346-370 `spheric_comps` */
+int sr_far_spheric_comps(int dtype, int native, void *spectrum1,
+                         void *spectrum2, void *spectrum3, const void *x,
+                         const void *y, const void *z, const void *ux,
+                         const void *uy, const void *uz, double wp,
+                         uint32_t itStart, uint32_t itEnd, uint32_t nSteps,
+                         const void *omega, const void *sinTheta,
+                         const void *cosTheta, const void *sinPhi,
+                         const void *cosPhi, uint32_t nOmega, uint32_t nTheta,
+                         uint32_t nPhi, double dt, uint32_t nSnaps,
+                         const uint32_t *itSnaps, void *stream);
+
+/* synchrad/kernel_farfield.cl:471-499 `spheric_comps_complex`
+ * (FormFactor is accepted and, as in the reference, not applied) */
+int sr_far_spheric_comps_complex(
+    int dtype, int native, void *spectrum1_re, void *spectrum1_im,
+    void *spectrum2_re, void *spectrum2_im, void *spectrum3_re,
+    void *spectrum3_im, const void *x, const void *y, const void *z,
+    const void *ux, const void *uy, const void *uz, double wp,
+    uint32_t itStart, uint32_t itEnd, uint32_t nSteps, const void *omega,
+    const void *sinTheta, const void *cosTheta, const void *sinPhi,
+    const void *cosPhi, uint32_t nOmega, uint32_t nTheta, uint32_t nPhi,
+    double dt, uint32_t nSnaps, const uint32_t *itSnaps,
+    const void *FormFactor, void *stream);
+
+/* synchrad/kernel_nearfield.cl:5-27 `total` */
+int sr_near_total(int dtype, int native, void *spectrum, const void *x,
+                  const void *y, const void *z, const void *ux, const void *uy,
+                  const void *uz, double wp, uint32_t itStart, uint32_t itEnd,
+                  uint32_t nSteps, const void *omega, const void *radius,
+                  const void *sinPhi, const void *cosPhi,
+                  double distanceToScreen, uint32_t nOmega, uint32_t nRadius,
+                  uint32_t nPhi, double dt, uint32_t nSnaps,
+                  const uint32_t *itSnaps, void *stream);
+
+/* synchrad/kernel_nearfield.cl:106-130 `cartesian_comps` */
+int sr_near_cartesian_comps(int dtype, int native, void *spectrum1,
+                            void *spectrum2, void *spectrum3, const void *x,
+                            const void *y, const void *z, const void *ux,
+                            const void *uy, const void *uz, double wp,
+                            uint32_t itStart, uint32_t itEnd, uint32_t nSteps,
+                            const void *omega, const void *radius,
+                            const void *sinPhi, const void *cosPhi,
+                            double distanceToScreen, uint32_t nOmega,
+                            uint32_t nRadius, uint32_t nPhi, double dt,
+                            uint32_t nSnaps, const uint32_t *itSnaps,
+                            void *stream);
+
+/* synchrad/kernel_nearfield.cl:216-244 `cartesian_comps_complex`
+ * (FormFactor is accepted and, as in the reference, not applied) */
+int sr_near_cartesian_comps_complex(
+    int dtype, int native, void *spectrum1_re, void *spectrum1_im,
+    void *spectrum2_re, void *spectrum2_im, void *spectrum3_re,
+    void *spectrum3_im, const void *x, const void *y, const void *z,
+    const void *ux, const void *uy, const void *uz, double wp,
+    uint32_t itStart, uint32_t itEnd, uint32_t nSteps, const void *omega,
+    const void *radius, const void *sinPhi, const void *cosPhi,
+    double distanceToScreen, uint32_t nOmega, uint32_t nRadius, uint32_t nPhi,
+    double dt, uint32_t nSnaps, const uint32_t *itSnaps,
+    const void *FormFactor, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SYNCHRAD_GB300_H */

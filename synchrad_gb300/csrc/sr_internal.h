@@ -1,0 +1,77 @@
+// Internal launch descriptors shared by the translation units of the library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sr {
+
+// Arguments of the plain-port kernels (one thread per spectral point, every
+// track of the batch in sequence).  `offsets == nullptr` selects the
+// single-track form of the reference kernels, with the scalars `*1` below.
+struct PortParams {
+  uint32_t n_tracks;
+  const int64_t *offsets;
+  const void *x, *y, *z, *ux, *uy, *uz;
+  const double *weight;
+  const uint32_t *it_start, *it_end, *snap_its;
+  uint32_t snap_stride, n_snaps;
+  double wp1;
+  uint32_t it_start1, it_end1, n_steps1;
+  double dt;
+  uint32_t n_omega, n_1, n_phi;
+  const void *omega, *axis1, *axis2, *sin_phi, *cos_phi, *form_factor;
+  double L;
+  void *out[6];
+};
+
+// mode: 0 far, 1 near; dtype: 0 f64, 1 f32.
+int launch_port(const PortParams &p, int mode, int comp, int dtype, bool native,
+                cudaStream_t stream);
+
+// Arguments of the mixed-precision far-field path.
+struct FarMixedParams {
+  // tracks
+  uint32_t n_tracks;
+  int track_f32;
+  int64_t total_steps;
+  const int64_t *offsets;
+  const void *x, *y, *z, *ux, *uy, *uz;
+  const double *weight;
+  const uint32_t *it_start, *it_end, *snap_its;
+  uint32_t snap_stride, n_snaps;
+  double dt;
+  // grid (FP64 axes)
+  uint32_t n_omega, n_theta, n_phi;
+  const double *omega, *sin_theta, *cos_theta, *sin_phi, *cos_phi,
+      *form_factor;
+  int comp;
+  int n_out;
+  // decomposition
+  uint32_t n_wtiles;   // omega tiles of 32*K points per direction
+  uint32_t n_groups;   // CTA-sized groups of warp tasks
+  uint32_t n_sub;      // track subsets
+  uint32_t n_items;    // n_groups * n_sub
+  // workspace
+  float4 *records;     // [total_steps][4]
+  double *partial;     // [n_sub][n_out][n_snaps][P]
+  int *status;
+  // outputs
+  double *out[6];
+};
+
+struct FarMixedConfig {
+  int K;        // points per lane
+  int W;        // warps per CTA
+  int n_sub;    // track subsets
+  int ctas_per_sm;
+};
+
+FarMixedConfig far_mixed_choose(uint32_t n_omega, uint32_t n_dirs,
+                                uint32_t n_tracks, int n_sm);
+size_t far_mixed_workspace(int64_t total_steps, uint64_t n_points, int n_out,
+                           uint32_t n_snaps, const FarMixedConfig &cfg);
+int launch_far_mixed(FarMixedParams p, const FarMixedConfig &cfg,
+                     void *workspace, size_t ws_bytes, cudaStream_t stream);
+
+}  // namespace sr

@@ -1,0 +1,61 @@
+"""CPU checks of the C ABI: the library builds, loads without a GPU, and exports
+every entry point declared in include/synchrad_gb300.h."""
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_entry_points():
+    text = (ROOT / "include" / "synchrad_gb300.h").read_text()
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t|const char \*)\s*(sr_\w+)\s*\(", text, re.M)))
+
+
+def test_header_declares_the_binding_table():
+    from synchrad_gb300 import _lib
+    assert declared_entry_points() == sorted(_lib.EXPORTS)
+
+
+def test_library_loads_and_exports_every_symbol():
+    from synchrad_gb300 import _lib
+    L = _lib.lib()
+    assert L.sr_version() >= 100
+    out = subprocess.run(["nm", "-D", "--defined-only", str(_lib.lib_path())],
+                         capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r" T (sr_\w+)", out))
+    for name in declared_entry_points():
+        assert name in exported, name
+        getattr(L, name)
+
+
+def test_last_error_is_empty_string_initially():
+    from synchrad_gb300 import _lib
+    assert _lib.lib().sr_last_error() in (b"",) or isinstance(_lib.lib().sr_last_error(), bytes)
+
+
+def test_pack_tracks_csr_on_cpu():
+    from synchrad_gb300.batch import pack_tracks
+    tr = [[np.arange(n, dtype=np.float64) + 10 * i for _ in range(6)] + [1.5 + i, 3]
+          for i, n in enumerate((5, 1, 7))]
+    b = pack_tracks(tr, np.float64, 2, 0.1, device="cpu", pinned=False)
+    assert b.offsets.tolist() == [0, 5, 6, 13]
+    assert b.coords[0][5:6].tolist() == [10.0]
+    assert b.it_end.tolist() == [5, 1, 7]
+    assert b.it_start.tolist() == [0, 0, 0]
+    assert b.snap_stride == 2
+    assert b.snap_its.tolist() == [2, 5, 0, 1, 3, 7]
+    g = pack_tracks(tr, np.float32, 3, 0.1, it_range=(0, 9), device="cpu", pinned=False)
+    assert g.it_start.tolist() == [3, 3, 3] and g.it_end.tolist() == [9, 9, 9]
+    assert g.snap_stride == 0 and g.snap_its.tolist() == [3, 6, 9]
+    assert g.coords[0].dtype.__str__() == "torch.float32"
+
+
+def test_pack_tracks_rejects_empty_track():
+    import pytest
+    from synchrad_gb300.batch import pack_tracks
+    tr = [[np.zeros(0) for _ in range(6)] + [1.0, 0]]
+    with pytest.raises(ValueError):
+        pack_tracks(tr, np.float64, 1, 0.1, device="cpu", pinned=False)
