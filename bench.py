@@ -1,0 +1,375 @@
+"""Benchmark of the SynchRad radiation integral on GB300.
+
+Metric: Gpt*steps/s = spectral points x sum over tracks of (steps - 1), per
+second, / 1e9, for the mixed-precision far-field path, with its relative L2
+error against the plain FP64 kernel stated alongside.
+
+Default workload (the configuration the metric is quoted on): 1024 electrons,
+gamma ~ N(400, 1%), planar undulator K = 1, offsets N(0, 2 um-eq), angles
+N(0, 0.05/gamma), 4000 steps each, weights U[0.5, 1.5]; grid 512 omega x 64
+theta x 64 phi over the first three harmonics; comp 'total'.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One "step" is one pass of the whole batch (every track, every point) through
+``sr_spectrum`` with the tracks already resident in HBM; L2 is flushed (a
+256 MB write) before every timed step.  ``e2e`` repeats the measurement through
+the public API ``SynchRad.calculate_spectrum`` from host (numpy) tracks, with
+the packing, host-to-device copies, kernels and the device-to-host read of the
+spectrum inside the timed region.
+
+Under torchrun (N > 1) each rank evaluates its own copy of the workload on its
+GPU (tracks are independent; weak scaling, no collective in the timed loop);
+the time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Gpt·steps/s (spectral pts × track steps), mixed vs FP64 at ≤1e-5 rel err"
+UNIT = "Gpt·steps/s"
+FLOPS_PER_UNIT = 14      # far field, mixed: 2 FMUL + 6 FFMA per point-step
+CANONICAL_FLOPS = 18     # the 3-component formulation's count
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--tracks", type=int, default=1024)
+    ap.add_argument("--track-steps", type=int, default=4000)
+    ap.add_argument("--grid", type=int, nargs=3, default=[512, 64, 64])
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) of SM clocks and throttle reasons."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: str):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_bench.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = np.array([float(r[1]) for r in rows])
+        smax = float(rows[0][2])
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4)
+                          if r[5 + i].lower().startswith("active")})
+        power = [float(r[3]) for r in rows if r[3] not in ("[N/A]", "")]
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(power) if power else None}
+
+
+def make_workload(args):
+    from synchrad_gb300 import workloads as wl
+    return wl.c2_far_mixed(n_tracks=args.tracks, n_steps=args.track_steps,
+                           grid=tuple(args.grid))
+
+
+def cpu_sample(w, n_tracks=4, sub=(16, 16)):
+    """A bounded sample of the workload for the CPU oracle: the first tracks on
+    the full omega axis and a sub-grid of directions."""
+    args = dict(w.args)
+    nO, nT, nP = args["grid"][-1]
+    (t0, t1), (p0, p1) = args["grid"][1], args["grid"][2]
+    # the first sub[0] theta nodes and sub[1] phi nodes of the full grid
+    dth = (t1 - t0) / (nT - 1) if nT > 1 else 0.0
+    dph = (p1 - p0) / nP
+    g = [args["grid"][0], (t0, t0 + dth * (sub[0] - 1)), (p0, p0 + dph * sub[1]),
+         (nO, sub[0], sub[1])]
+    return {"grid": g, "dtype": "double"}, [list(t) for t in w.tracks[:n_tracks]]
+
+
+def time_cpu_oracle(w, nthreads, n_tracks=4, sub=(16, 16), kind=None):
+    import oracle
+    from oracle import host
+    if kind is None:
+        kind = "reference" if oracle.ref_available() else "port"
+    lib_kind = "ref" if kind == "reference" else "port"
+    a, tracks = cpu_sample(w, n_tracks, sub)
+    t0 = time.perf_counter()
+    host.calculate_spectrum(a, tracks, w.time_step, comp="total", kind=lib_kind,
+                            nthreads=nthreads)
+    el = time.perf_counter() - t0
+    pts = int(np.prod(a["grid"][-1])) * sum(len(t[0]) - 1 for t in tracks)
+    return pts / el / 1e9, el, pts, kind
+
+
+def reference_arm(args):
+    """--impl reference: the reference's CPU implementation of the path."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    w = make_workload(args)
+    nth = os.cpu_count() or 1
+    vals = []
+    kind = None
+    for i in range(args.warmup + args.steps):
+        v, el, pts, kind = time_cpu_oracle(w, nth, n_tracks=2, sub=(8, 16))
+        if i >= args.warmup:
+            vals.append((v, el))
+    v = float(np.median([x[0] for x in vals]))
+    ms = float(np.mean([x[1] for x in vals])) * 1e3
+    sample = (f"2 tracks x 4000 steps on the full 512-omega axis x 8 theta x 16 phi "
+              f"(the first nodes of the grid), FP64, {nth} threads")
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": w.name, "sample": sample},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": nth,
+                             "kind": "reference" if kind == "reference" else "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        dist = None
+    device = torch.device("cuda", local if ws > 1 else 0)
+    torch.cuda.set_device(device)
+
+    from oracle import host as ohost
+    from synchrad_gb300 import _lib
+    from synchrad_gb300.batch import Workspace, make_grid, pack_tracks, run_spectrum
+    from synchrad_gb300.calc import SynchRad
+
+    L = _lib.lib()
+    w = make_workload(args)
+    a = ohost.init_args(dict(w.args, dtype="double"))
+    nO, nT, nP = (int(v) for v in a["gridNodeNums"])
+    P = nO * nT * nP
+    grid = make_grid("far", ohost.device_axes(a), (nO, nT, nP), torch.float64, device)
+    batch = pack_tracks(w.tracks, np.float64, 1, w.time_step, device=device)
+    out = torch.zeros((1, nP, nT, nO), dtype=torch.float64, device=device)
+    wsp = Workspace(device)
+    pt_steps = w.pt_steps
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+    stream = torch.cuda.current_stream(device)
+
+    def one_step():
+        flush.fill_(1.0)
+        out.zero_()
+        run_spectrum(batch, grid, "total", _lib.SR_PREC_MIXED, [out], workspace=wsp,
+                     stream=stream)
+
+    for _ in range(args.warmup):
+        one_step()
+    torch.cuda.synchronize()
+    _lib.check(L.sr_timing_read(None, None))  # clear
+    _lib.check(L.sr_timing_enable(1))
+    try:
+        gpu_id = "GPU-" + str(torch.cuda.get_device_properties(device).uuid)
+    except Exception:
+        gpu_id = str(device.index)
+    with ClockSampler(gpu_id) as clocks:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            one_step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    _lib.check(L.sr_timing_enable(0))
+    kern_ms = ctypes.c_double(0)
+    kern_n = ctypes.c_int(0)
+    _lib.check(L.sr_timing_read(ctypes.byref(kern_ms), ctypes.byref(kern_n)))
+    _lib.check(L.sr_workspace_status(ctypes.c_void_p(wsp.buf.data_ptr()),
+                                     ctypes.c_void_p(stream.cuda_stream)))
+    elapsed_ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([elapsed_ms], device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    ms_per_step = elapsed_ms / args.steps
+    value = pt_steps * ws * args.steps / (elapsed_ms * 1e-3) / 1e9
+    mixed_spec = out.clone()
+
+    # --- roofline of the dominant kernel (far_mixed_kernel) ---
+    tf_s = ctypes.c_double(0)
+    tf_p = ctypes.c_double(0)
+    _lib.check(L.sr_probe_fp32_peak(ctypes.byref(tf_s), ctypes.byref(tf_p),
+                                    ctypes.c_void_p(stream.cuda_stream)))
+    kern_avg_ms = kern_ms.value / max(kern_n.value, 1)
+    achieved = pt_steps * FLOPS_PER_UNIT / (kern_avg_ms * 1e-3) / 1e12
+    peak = max(tf_s.value, tf_p.value)
+    clk = clocks.summary()
+    roofline = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak if peak else None,
+                "traffic": None,
+                "kernel": "far_mixed_kernel<16,8>",
+                "kernel_ms_avg": kern_avg_ms,
+                "flops_per_unit": FLOPS_PER_UNIT,
+                "frac_canonical_18_flops": (achieved * CANONICAL_FLOPS / FLOPS_PER_UNIT / peak
+                                            if peak else None),
+                "peak_source": ("measured on this GPU by sr_probe_fp32_peak (FFMA / FFMA2 "
+                                f"throughput: {tf_s.value:.1f} / {tf_p.value:.1f} TFLOP/s); "
+                                "MEASURED_PEAKS.json has no FP32 figure"),
+                "peak_nominal_at_max_clock": (2 * 128 * torch.cuda.get_device_properties(device)
+                                              .multi_processor_count
+                                              * (clk.get("sm_max_mhz") or 2070) * 1e6 / 1e12)}
+
+    # --- accuracy and throughput of the plain FP64 kernel on a track subset ---
+    fp64 = None
+    if not args.no_fp64:
+        sub_tr = w.tracks[:2]
+        sb = pack_tracks(sub_tr, np.float64, 1, w.time_step, device=device)
+        o64 = torch.zeros_like(out)
+        omx = torch.zeros_like(out)
+        run_spectrum(sb, grid, "total", _lib.SR_PREC_MIXED, [omx], workspace=wsp)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        run_spectrum(sb, grid, "total", _lib.SR_PREC_DOUBLE, [o64], workspace=wsp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t64 = e0.elapsed_time(e1)
+        pts64 = P * sum(len(t[0]) - 1 for t in sub_tr)
+        ref = o64.cpu().numpy().ravel()
+        got = omx.cpu().numpy().ravel()
+        rel = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+        floor = 1e-3 * np.abs(ref).max()
+        big = np.abs(ref) > floor
+        maxrel = float(np.max(np.abs(got[big] - ref[big]) / np.abs(ref[big])))
+        fp64 = {"value": pts64 / (t64 * 1e-3) / 1e9, "unit": UNIT,
+                "sample": "first 2 tracks, full grid, plain FP64 kernel",
+                "mixed_speedup": value / ws / (pts64 / (t64 * 1e-3) / 1e9),
+                "rel_l2_mixed_vs_fp64": rel,
+                "max_rel_mixed_vs_fp64": maxrel,
+                "max_rel_floor": "points above 1e-3 of the spectrum maximum"}
+
+    # --- end to end through the public API, host tracks ---
+    e2e = None
+    if not args.no_e2e:
+        n_e2e = args.e2e_steps or args.steps
+        calc = SynchRad({"grid": w.args["grid"], "dtype": "mixed"})
+        host_tracks = [list(t) for t in w.tracks]
+        calc.calculate_spectrum(host_tracks, timeStep=w.time_step, verbose=False)  # warm
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(n_e2e):
+            calc.calculate_spectrum(host_tracks, timeStep=w.time_step, verbose=False)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        if dist:
+            t = torch.tensor([el], device=device)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            el = float(t.item())
+        e2e_spec = calc.Data["radiation"]["total"]
+        host_ref = mixed_spec.cpu().numpy().swapaxes(-1, -3)
+        e2e = {"value": pt_steps * ws * n_e2e / el / 1e9, "unit": UNIT,
+               "h2d_bytes_per_step": int(batch.h2d_bytes),
+               "d2h_bytes_per_step": int(P * 8),
+               "steps": n_e2e, "ms_per_step": el / n_e2e * 1e3,
+               "api": "SynchRad.calculate_spectrum (numpy tracks in, numpy spectrum out)",
+               "matches_device_run": bool(np.allclose(e2e_spec, host_ref, rtol=1e-12, atol=0))}
+
+    cpu = None
+    if not args.no_cpu and rank == 0 and ws == 1:
+        nth = os.cpu_count() or 1
+        v, el, pts, kind = time_cpu_oracle(w, nth)
+        cpu = {"value": v, "unit": UNIT, "cores": nth, "kind": kind,
+               "sample": f"first 4 tracks x 4000 steps on the full 512-omega axis x 16 theta "
+                         f"x 16 phi, FP64, {nth} threads, {el:.1f} s"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32 (mixed: double-float phase, compensated FP32 sums, FP64 spectrum)",
+                "data": "synthetic",
+                "config": {"workload": w.name, "n_tracks": len(w.tracks),
+                           "steps_per_track": args.track_steps, "grid": list(args.grid),
+                           "comp": "total", "pt_steps_per_step": pt_steps,
+                           "l2": "flushed before every timed step (256 MB write, counted); "
+                                 "step records (262 MB) exceed L2",
+                           "parallelism": f"replicas x{ws} (tracks independent)"},
+                "e2e": e2e, "gpu_launches": 3 * args.steps * 1,
+                "clocks": clk, "roofline": roofline, "cpu_baseline": cpu, "fp64_port": fp64}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

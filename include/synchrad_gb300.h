@@ -132,6 +132,23 @@ const char *sr_last_error(void);
 int sr_version(void);
 
 /* ---------------------------------------------------------------------------
+ * Diagnostics.  These have no counterpart in the reference; the benchmark uses
+ * them for its roofline figures.
+ * ------------------------------------------------------------------------- */
+
+/* While enabled, every sr_spectrum / per-track call records CUDA events around
+ * its dominant kernel on the call's stream. */
+int sr_timing_enable(int enable);
+
+/* Waits for the recorded events, returns their summed duration (ms) and count,
+ * and clears the record. */
+int sr_timing_read(double *total_ms, int *n_launches);
+
+/* Measures this device's FP32 fused-multiply-add throughput (TFLOP/s, 2 flops
+ * per FMA) with scalar FFMA and with packed FFMA2 instructions. */
+int sr_probe_fp32_peak(double *tflops_scalar, double *tflops_packed, void *stream);
+
+/* ---------------------------------------------------------------------------
  * Per-track entry points: the reference's OpenCL kernels, one launch each.
  *
  * Same argument order and meaning as the kernels in

@@ -24,6 +24,7 @@ SOURCES = {
     "sr_api.cu": [],
     "sr_port.cu": ["--fmad=false"],
     "sr_far_mixed.cu": [],
+    "sr_diag.cu": [],
 }
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",

@@ -89,7 +89,8 @@ EXPORTS = (
     "sr_version", "sr_far_total", "sr_far_cartesian_comps",
     "sr_far_cartesian_comps_complex", "sr_far_spheric_comps",
     "sr_far_spheric_comps_complex", "sr_near_total", "sr_near_cartesian_comps",
-    "sr_near_cartesian_comps_complex",
+    "sr_near_cartesian_comps_complex", "sr_timing_enable", "sr_timing_read",
+    "sr_probe_fp32_peak",
 )
 
 _lock = threading.Lock()
@@ -109,6 +110,12 @@ def _declare(L: ctypes.CDLL) -> None:
     L.sr_last_error.argtypes = []
     L.sr_version.restype = i32
     L.sr_version.argtypes = []
+    L.sr_timing_enable.restype = i32
+    L.sr_timing_enable.argtypes = [i32]
+    L.sr_timing_read.restype = i32
+    L.sr_timing_read.argtypes = [ctypes.POINTER(dbl), ctypes.POINTER(i32)]
+    L.sr_probe_fp32_peak.restype = i32
+    L.sr_probe_fp32_peak.argtypes = [ctypes.POINTER(dbl), ctypes.POINTER(dbl), vp]
     track = [vp] * 6 + [dbl, u32, u32, u32]
     far_axes = [vp] * 5 + [u32, u32, u32, dbl, u32, vp]
     near_axes = [vp] * 4 + [dbl, u32, u32, u32, dbl, u32, vp]

@@ -664,7 +664,10 @@ int launch_far_mixed(FarMixedParams p, const FarMixedConfig &cfg, void *ws, size
   const int occ = occupancy(cfg.K, cfg.W);
   int grid = n_sm * occ;
   if ((uint32_t)grid > p.n_items) grid = (int)p.n_items;
+  void *tok = nullptr;
+  timing_record(stream, true, &tok);
   int rc = dispatch_k<8>(cfg.K, p, grid, stream);
+  timing_record(stream, false, &tok);
   if (rc) return rc;
   const uint64_t total = (uint64_t)p.n_out * p.n_snaps * P;
   uint64_t nb = (total + 255) / 256;

@@ -25,6 +25,9 @@ struct PortParams {
   void *out[6];
 };
 
+// Optional CUDA-event timing of the dominant kernel of a call (sr_diag.cu).
+void timing_record(cudaStream_t s, bool start, void **token);
+
 // mode: 0 far, 1 near; dtype: 0 f64, 1 f32.
 int launch_port(const PortParams &p, int mode, int comp, int dtype, bool native,
                 cudaStream_t stream);

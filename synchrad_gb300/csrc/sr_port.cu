@@ -290,9 +290,17 @@ int launch_typed(const PortParams &p, int mode, int comp, cudaStream_t s) {
 int launch_port(const PortParams &p, int mode, int comp, int dtype, bool native,
                 cudaStream_t stream) {
   if ((uint64_t)p.n_omega * p.n_1 * p.n_phi == 0) return SR_OK;
-  if (dtype == SR_DTYPE_F64) return launch_typed<double, false>(p, mode, comp, stream);
-  if (native) return launch_typed<float, true>(p, mode, comp, stream);
-  return launch_typed<float, false>(p, mode, comp, stream);
+  void *tok = nullptr;
+  timing_record(stream, true, &tok);
+  int rc;
+  if (dtype == SR_DTYPE_F64)
+    rc = launch_typed<double, false>(p, mode, comp, stream);
+  else if (native)
+    rc = launch_typed<float, true>(p, mode, comp, stream);
+  else
+    rc = launch_typed<float, false>(p, mode, comp, stream);
+  timing_record(stream, false, &tok);
+  return rc;
 }
 
 }  // namespace sr
