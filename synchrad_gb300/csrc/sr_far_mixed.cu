@@ -17,23 +17,26 @@
 //    n_x, n_y): tau = q + (1 - cos theta) z - n_x x - n_y y, free of the
 //    cancellation of t - n.x.
 //  * exp(i omega_j tau) along a lane's K consecutive omega points is a
-//    rotation recurrence z_{j+1} = z_j R, R = exp(i domega tau), with an exact
-//    double-float reseed of the first point at every step; two points are
-//    advanced at once with packed FFMA2/FMUL2.
+//    rotation recurrence z_{j+1} = z_j R, R = exp(i domega tau), run as two
+//    packed chains (FFMA2/FMUL2 on point pairs) from an exact double-float
+//    reseed of the lane's first point at every step;
 //  * the |dphase| < pi mask is decided per step from |omega| |dtau| with a
 //    guard band; inside the band the reference's FP64 expression is evaluated
 //    bit for bit from the original track data.
-//  * sums are FP32 inside a TMA stage of steps and folded into compensated
-//    (Knuth TwoSum) FP32 pairs in shared memory; per-track results are formed
-//    and accumulated in FP64.
+//  * sums are FP32 for 1024 steps at a time and then folded into compensated
+//    (Knuth TwoSum) FP32 pairs kept in an L2-resident workspace; per-track
+//    results are formed and accumulated in FP64.
 //
-// Work decomposition: a warp owns one direction and an omega tile of 32*K
-// points (lane l: points tile*32K + l*K .. +K-1); a CTA of W warps owns W
+// Work decomposition: a warp owns 32/L directions and, for each, an omega
+// tile of L*K points (lane: K consecutive points); a CTA of W warps owns W
 // consecutive warp tasks and loops over a contiguous subset of the tracks.
 // Track records are streamed through shared memory by 1-D bulk TMA copies
-// (cp.async.bulk + mbarrier, double buffered) and reused by every warp.  Each
-// (task group, track subset) item writes its own partial spectrum; a final
-// kernel adds the subsets in fixed order, so results are deterministic.
+// (cp.async.bulk + mbarrier, double buffered) and reused by every warp; the
+// per-(direction, step) setup is computed once per warp and broadcast through
+// shared memory.  Each (task group, track subset) item writes its own partial
+// spectrum; a final kernel adds the subsets in fixed order, so results are
+// deterministic.
+#include <algorithm>
 #include <cmath>
 
 #include "sr_common.cuh"
@@ -43,6 +46,7 @@ namespace sr {
 namespace {
 
 constexpr int kStage = 128;         // steps per TMA stage
+constexpr int kFoldStages = 8;      // FP32 sums fold into compensated pairs every 1024 steps
 constexpr int kRecF4 = 4;           // float4 per step record (64 bytes)
 constexpr float kPiLo = 3.14159265358979f * (1.0f - 4e-6f);
 constexpr float kPiHi = 3.14159265358979f * (1.0f + 4e-6f);
@@ -153,23 +157,69 @@ __device__ __noinline__ bool exact_mask(const FarMixedParams &p, int64_t base, u
   return fabs(__dsub_rn(ph, prev)) < M_PI;
 }
 
-template <int K, int W>
-struct Smem {
-  float4 stage[2][kStage * kRecF4];    // 2 x 8 KB
-  uint64_t bar[2];
-  uint64_t pad_[2];
-  float4 setup[W][32][3];              // per-step broadcast values
-  float kahan[W][K][8][32];            // (sum, comp) x (th re, th im, ph re, ph im)
-  float2 omega_df[W][32 * K];          // omega table for non-uniform lanes
+// Per-direction constants, written once per work item.
+struct DirConst {
+  double sT, cT, sPh, cPh, n0, n1;  // n = (n0, n1, cT) rounded as the reference does
+  float dc_h, dc_l, dsx_h, dsx_l, dsy_h, dsy_l;  // 1 - cos(theta), n0, n1 as double-floats
+  float f_c, f_sx, f_sy, f_cz;                   // the same in FP32
+  float thx, thy, thz, phx, phy;                 // theta-hat, phi-hat
+  float tprev_h, tprev_l;                        // tau of the step before the current chunk
+  float pad_;
 };
 
+constexpr int kMaxDpw = 8;  // directions per warp (omega tiles narrower than 32 lanes)
+
+template <int W>
+struct SmemFixed {
+  float4 stage[2][kStage * kRecF4];  // 2 x 8 KB of step records
+  uint64_t bar[2];
+  uint64_t pad_[2];
+  DirConst dc[W][kMaxDpw];
+  // followed by float4 setup[W][32][dpw][3]
+};
+
+// exp(i 2 pi w tau) for a double-float frequency in revolutions: the phase is
+// formed in double-float, its whole revolutions are dropped (p - rint(p) is
+// exact), and the fraction goes to the SFU sin/cos.
+__device__ __forceinline__ void phasor_rev(float wh, float wl, float th, float tl, float &s,
+                                           float &c) {
+  const float p = wh * th;
+  float e = __fmaf_rn(wh, th, -p);
+  e = __fmaf_rn(wh, tl, e);
+  e = __fmaf_rn(wl, th, e);
+  const float n = rintf(p);
+  const float f = (p - n) + e;
+  __sincosf(f * 6.28318530717958648f, &s, &c);
+}
+
+// (zr + i zi) * (rc + i rs) for two points at once.
+__device__ __forceinline__ void rot2(float2 zr, float2 zi, float rc, float rs, float2 &or_,
+                                     float2 &oi) {
+  const float2 u = __fmul2_rn(zi, make_float2(-rs, -rs));
+  const float2 v = __fmul2_rn(zr, make_float2(rs, rs));
+  or_ = __ffma2_rn(zr, make_float2(rc, rc), u);
+  oi = __ffma2_rn(zi, make_float2(rc, rc), v);
+}
+
+__device__ __forceinline__ void cmul(float ar, float ai, float br, float bi, float &cr,
+                                     float &ci) {
+  cr = ar * br - ai * bi;
+  ci = ar * bi + ai * br;
+}
+
+// Kernel of the mixed-precision far field.  K points per lane (two packed
+// rotation chains of K/2), L lanes per direction, 32/L directions per warp.
 template <int K, int W>
 __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) {
-  static_assert(K % 2 == 0 && K >= 2 && K <= 16, "K");
+  static_assert(K % 4 == 0 && K >= 4 && K <= 32, "K");
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  Smem<K, W> &sm = *reinterpret_cast<Smem<K, W> *>(smem_raw);
+  SmemFixed<W> &sm = *reinterpret_cast<SmemFixed<W> *>(smem_raw);
+  const int dpw = (int)p.dpw, L = 32 / dpw;
+  float4 *setup_all = reinterpret_cast<float4 *>(smem_raw + sizeof(SmemFixed<W>));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  constexpr int KP = K / 2;
+  const int dsub = lane / L, ll = lane % L;
+  float4 *setup = setup_all + (size_t)warp * 32 * dpw * 3;
+  constexpr int KP = K / 2, HP = KP / 2;
 
   if (threadIdx.x == 0) {
     mbar_init(&sm.bar[0], 1);
@@ -181,55 +231,60 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
   const uint32_t nO = p.n_omega, nT = p.n_theta;
   const uint32_t n_dirs = nT * p.n_phi;
   const uint64_t P = (uint64_t)nO * n_dirs;
-  const uint32_t n_wt = n_dirs * p.n_wtiles;
+  const uint32_t n_groups_dir = (n_dirs + dpw - 1) / dpw;  // direction groups
+  const uint32_t n_wt = n_groups_dir * p.n_wtiles;         // warp tasks
   const double dw_glob = (nO > 1) ? (p.omega[nO - 1] - p.omega[0]) / (double)(nO - 1) : 0.0;
   const df d_dw = df_from_double(dw_glob);
-
+  const double inv2pi = 0.15915494309189533577;
+  float *outer = p.outer + ((size_t)blockIdx.x * W + warp) * K * 8 * 32;
   uint32_t stage_no = 0;  // running stage counter (mbarrier phase bookkeeping)
-  bool pending = false;   // a copy for stage_no is in flight
 
   for (uint32_t item = blockIdx.x; item < p.n_items; item += gridDim.x) {
     const uint32_t sub = item / p.n_groups, grp = item % p.n_groups;
     const uint32_t wt = grp * W + warp;
-    const bool active = wt < n_wt;
-    const uint32_t dir = active ? wt / p.n_wtiles : 0u;
-    const uint32_t tile = active ? wt % p.n_wtiles : 0u;
-    const uint32_t iT = dir % nT, iP = dir / nT;
-    const int j0 = (int)(tile * 32u * K) + lane * K;
+    const bool active_w = wt < n_wt;
+    const uint32_t dgrp = active_w ? wt / p.n_wtiles : 0u;
+    const uint32_t tile = active_w ? wt % p.n_wtiles : 0u;
+    const uint32_t dir_raw = dgrp * dpw + dsub;
+    const bool active = active_w && dir_raw < n_dirs;
+    const uint32_t dir = active ? dir_raw : 0u;
+    const int j0 = (int)(tile * (uint32_t)(L * K)) + ll * K;
     const int nv = active ? max(0, min(K, (int)nO - j0)) : 0;
 
-    // Direction constants: n = (sinT cosP, sinT sinP, cosT) as the reference
-    // rounds them, theta-hat, phi-hat.
-    const double sT = p.sin_theta[iT], cT = p.cos_theta[iT];
-    const double sPh = p.sin_phi[iP], cPh = p.cos_phi[iP];
-    const double n0d = sT * cPh, n1d = sT * sPh, n2d = cT;
-    const df d_c = df_from_double(1.0 - cT), d_sx = df_from_double(n0d),
-             d_sy = df_from_double(n1d);
-    const float f_c = (float)(1.0 - cT), f_sx = (float)n0d, f_sy = (float)n1d,
-                f_cz = (float)cT;
-    const float thx = (float)(cT * cPh), thy = (float)(cT * sPh), thz = (float)(-sT);
-    const float phx = (float)(-sPh), phy = (float)cPh;
+    if (ll == 0) {
+      const uint32_t iT = dir % nT, iP = dir / nT;
+      DirConst &d = sm.dc[warp][dsub];
+      d.sT = p.sin_theta[iT];
+      d.cT = p.cos_theta[iT];
+      d.sPh = p.sin_phi[iP];
+      d.cPh = p.cos_phi[iP];
+      d.n0 = d.sT * d.cPh;
+      d.n1 = d.sT * d.sPh;
+      const df c = df_from_double(1.0 - d.cT), sx = df_from_double(d.n0),
+               sy = df_from_double(d.n1);
+      d.dc_h = c.hi; d.dc_l = c.lo; d.dsx_h = sx.hi; d.dsx_l = sx.lo;
+      d.dsy_h = sy.hi; d.dsy_l = sy.lo;
+      d.f_c = (float)(1.0 - d.cT); d.f_sx = (float)d.n0; d.f_sy = (float)d.n1;
+      d.f_cz = (float)d.cT;
+      d.thx = (float)(d.cT * d.cPh); d.thy = (float)(d.cT * d.sPh); d.thz = (float)(-d.sT);
+      d.phx = (float)(-d.sPh); d.phy = (float)d.cPh;
+    }
 
-    // Lane omega constants and uniformity of its chunk.
+    // Lane omega constants (revolutions) and uniformity of its chunk.
     const double w0d = nv > 0 ? p.omega[j0] : 0.0;
-    const df d_w0 = df_from_double(w0d);
+    const df d_w0 = df_from_double(w0d * inv2pi);
     bool uniform = true;
     float wabs_min = 3.0e38f, wabs_max = 0.f;
-    for (int m = 0; m < K; ++m) {
-      if (m < nv) {
-        const double wm = p.omega[j0 + m];
-        const double pred = w0d + (double)m * dw_glob;
-        if (fabs(wm - pred) > 1e-12 * fabs(wm) + 1e-300) uniform = false;
-        const float a = (float)fabs(wm);
-        wabs_min = fminf(wabs_min, a);
-        wabs_max = fmaxf(wabs_max, a);
-        const df dm = df_from_double(wm);
-        sm.omega_df[warp][lane * K + m] = make_float2(dm.hi, dm.lo);
-      } else {
-        sm.omega_df[warp][lane * K + m] = make_float2(0.f, 0.f);
-      }
+    for (int m = 0; m < nv; ++m) {
+      const double wm = p.omega[j0 + m];
+      const double pred = w0d + (double)m * dw_glob;
+      if (fabs(wm - pred) > 1e-12 * fabs(wm) + 1e-300) uniform = false;
+      const float a = (float)fabs(wm);
+      wabs_min = fminf(wabs_min, a);
+      wabs_max = fmaxf(wabs_max, a);
     }
     if (nv == 0) { wabs_min = 0.f; wabs_max = 0.f; }
+    __syncwarp();
 
     uint32_t t0, t1;
     subset_tracks(p, sub, t0, t1);
@@ -238,14 +293,12 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
     uint32_t cur_t = t0;
     while (cur_t < t1 && track_body(p, cur_t) == 0) ++cur_t;
     if (threadIdx.x == 0 && cur_t < t1) {
-      const uint32_t nb = track_body(p, cur_t);
-      const uint32_t cnt = min((uint32_t)kStage, nb);
+      const uint32_t cnt = min((uint32_t)kStage, track_body(p, cur_t));
       const int b = stage_no & 1;
       fence_proxy_async();
       mbar_arrive_expect_tx(&sm.bar[b], cnt * 64u);
       bulk_g2s(sm.stage[b], p.records + (p.offsets[cur_t]) * kRecF4, cnt * 64u, &sm.bar[b]);
     }
-    pending = cur_t < t1;
 
     for (uint32_t t = t0; t < t1; ++t) {
       const int64_t base = p.offsets[t];
@@ -258,36 +311,53 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
 
       float2 aTr[KP], aTi[KP], aPr[KP], aPi[KP];
 #pragma unroll
-      for (int q = 0; q < KP; ++q) {
-        aTr[q] = aTi[q] = aPr[q] = aPi[q] = make_float2(0.f, 0.f);
-      }
-#pragma unroll
-      for (int m = 0; m < K; ++m)
-#pragma unroll
-        for (int v = 0; v < 8; ++v) sm.kahan[warp][m][v][lane] = 0.f;
+      for (int q = 0; q < KP; ++q) aTr[q] = aTi[q] = aPr[q] = aPi[q] = make_float2(0.f, 0.f);
+      bool outer_live = false;  // outer compensated sums hold this track's data
 
-      // Snapshot write: A = compensated outer sum + inner sum, per comp, FP64.
-      auto flush = [&](uint32_t ksnap) {
+      // Folds the FP32 sums into the compensated pairs in the workspace.
+      auto fold = [&]() {
         if (!active) return;
-        const double wpdt2 = wp * p.dt * p.dt;
-        const double wpdt = sqrt(wp) * p.dt;
-        const double thxd = cT * cPh, thyd = cT * sPh, thzd = -sT;
-        const double phxd = -sPh, phyd = cPh;
 #pragma unroll
         for (int m = 0; m < K; ++m) {
-          if (m >= nv) continue;
           const int q = m >> 1;
-          const float itr = (m & 1) ? aTr[q].y : aTr[q].x;
-          const float iti = (m & 1) ? aTi[q].y : aTi[q].x;
-          const float ipr = (m & 1) ? aPr[q].y : aPr[q].x;
-          const float ipi = (m & 1) ? aPi[q].y : aPi[q].x;
-          const float *kh = &sm.kahan[warp][m][0][lane];
-          const double Ar = (double)kh[0 * 32] + (double)kh[4 * 32] + (double)itr;
-          const double Ai = (double)kh[1 * 32] + (double)kh[5 * 32] + (double)iti;
-          const double Br = (double)kh[2 * 32] + (double)kh[6 * 32] + (double)ipr;
-          const double Bi = (double)kh[3 * 32] + (double)kh[7 * 32] + (double)ipi;
+          const float v[4] = {(m & 1) ? aTr[q].y : aTr[q].x, (m & 1) ? aTi[q].y : aTi[q].x,
+                              (m & 1) ? aPr[q].y : aPr[q].x, (m & 1) ? aPi[q].y : aPi[q].x};
+          float *o = outer + (size_t)m * 8 * 32 + lane;
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            if (outer_live) {
+              const df e = two_sum(o[c * 32], v[c]);
+              o[c * 32] = e.hi;
+              o[(c + 4) * 32] += e.lo;
+            } else {
+              o[c * 32] = v[c];
+              o[(c + 4) * 32] = 0.f;
+            }
+          }
+        }
+        outer_live = true;
+#pragma unroll
+        for (int q = 0; q < KP; ++q) aTr[q] = aTi[q] = aPr[q] = aPi[q] = make_float2(0.f, 0.f);
+      };
+
+      // Snapshot write: A = the compensated sums, per comp, in FP64.
+      auto flush = [&](uint32_t ksnap) {
+        fold();
+        if (!active) return;
+        const DirConst &d = sm.dc[warp][dsub];
+        const double wpdt2 = wp * p.dt * p.dt;
+        const double wpdt = sqrt(wp) * p.dt;
+        const double thxd = d.cT * d.cPh, thyd = d.cT * d.sPh, thzd = -d.sT;
+        const double phxd = -d.sPh, phyd = d.cPh;
+        double *part = p.partial + ((uint64_t)sub * p.n_out * p.n_snaps) * P;
+#pragma unroll 1
+        for (int m = 0; m < nv; ++m) {
+          const float *o = outer + (size_t)m * 8 * 32 + lane;
+          const double Ar = (double)o[0 * 32] + (double)o[4 * 32];
+          const double Ai = (double)o[1 * 32] + (double)o[5 * 32];
+          const double Br = (double)o[2 * 32] + (double)o[6 * 32];
+          const double Bi = (double)o[3 * 32] + (double)o[7 * 32];
           const uint64_t gti = (uint64_t)(j0 + m) + (uint64_t)nO * dir;
-          double *part = p.partial + ((uint64_t)sub * p.n_out * p.n_snaps) * P;
           auto add = [&](int c, double v) {
             part[((uint64_t)c * p.n_snaps + ksnap) * P + gti] += v;
           };
@@ -328,8 +398,8 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
         }
       };
 
-      df tprev = {0.f, 0.f};  // tau of the previous step (track start: 0 phase)
-      for (uint32_t s0 = 0; s0 < n_body; s0 += kStage) {
+      uint32_t stage_in_track = 0;
+      for (uint32_t s0 = 0; s0 < n_body; s0 += kStage, ++stage_in_track) {
         const uint32_t cnt = min((uint32_t)kStage, n_body - s0);
         const int b = stage_no & 1;
         // Issue the next stage (this track or the next non-empty one of the item).
@@ -341,13 +411,12 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
             while (nt < t1 && track_body(p, nt) == 0) ++nt;
           }
           if (nt < t1) {
-            const uint32_t nb = track_body(p, nt);
-            const uint32_t ncnt = min((uint32_t)kStage, nb - ns0);
+            const uint32_t ncnt = min((uint32_t)kStage, track_body(p, nt) - ns0);
             const int nbuf = (stage_no + 1) & 1;
             fence_proxy_async();
             mbar_arrive_expect_tx(&sm.bar[nbuf], ncnt * 64u);
-            bulk_g2s(sm.stage[nbuf], p.records + (p.offsets[nt] + ns0) * kRecF4,
-                     ncnt * 64u, &sm.bar[nbuf]);
+            bulk_g2s(sm.stage[nbuf], p.records + (p.offsets[nt] + ns0) * kRecF4, ncnt * 64u,
+                     &sm.bar[nbuf]);
           }
         }
         const bool ok = mbar_wait_bounded(&sm.bar[b], (stage_no >> 1) & 1, kWaitLimitNs);
@@ -363,123 +432,167 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
         }
         const float4 *stg = sm.stage[b];
 
-        if (active) {
+        if (active_w) {
           for (uint32_t c0 = 0; c0 < cnt; c0 += 32) {
             const uint32_t mcnt = min(32u, cnt - c0);
-            // ---- per-step setup: lane l -> step s0 + c0 + l ----
+            // ---- per-step setup: lane l -> step s0 + c0 + l, every direction ----
             {
               const uint32_t l = (uint32_t)lane < mcnt ? (uint32_t)lane : mcnt - 1;
               const float4 r0 = stg[(c0 + l) * kRecF4 + 0];
               const float4 r1 = stg[(c0 + l) * kRecF4 + 1];
               const float4 r2 = stg[(c0 + l) * kRecF4 + 2];
               const float4 r3 = stg[(c0 + l) * kRecF4 + 3];
-              // tau = q + (1 - cos th) z - n_x x - n_y y   (double-float)
-              df tau = df{r0.x, r0.y};
-              tau = df_add(tau, df_mul(d_c, df{r1.z, r1.w}));
-              df nx = df_mul(d_sx, df{r0.z, r0.w});
-              df ny = df_mul(d_sy, df{r1.x, r1.y});
-              tau = df_add(tau, df{-nx.hi, -nx.lo});
-              tau = df_add(tau, df{-ny.hi, -ny.lo});
-              // previous step's tau (lane 0: carried, or 0-phase at track start)
-              float ph = __shfl_up_sync(0xffffffffu, tau.hi, 1);
-              float pl = __shfl_up_sync(0xffffffffu, tau.lo, 1);
-              if (lane == 0) { ph = tprev.hi; pl = tprev.lo; }
               const bool first = (s0 + c0 + l) == 0;
-              const float dtau = first ? (tau.hi + tau.lo) : ((tau.hi - ph) + (tau.lo - pl));
-              // amplitude on theta-hat / phi-hat
-              const float D = r2.w + f_c * r2.z - f_sx * r2.x - f_sy * r2.y;
-              const float c2 = __frcp_rn(D);
-              const float an = f_sx * r3.x + f_sy * r3.y + f_cz * r3.z;
-              const float c1 = an * c2 * c2;
-              const float tb = thx * r2.x + thy * r2.y + thz * r2.z;
-              const float ta = thx * r3.x + thy * r3.y + thz * r3.z;
-              const float pb = phx * r2.x + phy * r2.y;
-              const float pa = phx * r3.x + phy * r3.y;
-              const float amp_t = -(c1 * tb + c2 * ta);
-              const float amp_p = -(c1 * pb + c2 * pa);
-              // rotation between neighbouring omega points
-              const df rp = df_mul_raw(d_dw, tau);
-              const float rr = reduce_2pi(rp.hi, rp.lo);
-              float Rs, Rc;
-              sincosf(rr, &Rs, &Rc);
-              const float R2c = Rc * Rc - Rs * Rs, R2s = 2.f * Rc * Rs;
-              sm.setup[warp][lane][0] = make_float4(tau.hi, tau.lo, amp_t, amp_p);
-              sm.setup[warp][lane][1] = make_float4(Rc, Rs, R2c, R2s);
-              sm.setup[warp][lane][2] = make_float4(fabsf(dtau), 0.f, 0.f, 0.f);
-              const float th_last = __shfl_sync(0xffffffffu, tau.hi, mcnt - 1);
-              const float tl_last = __shfl_sync(0xffffffffu, tau.lo, mcnt - 1);
-              tprev = df{th_last, tl_last};
+              for (int dd = 0; dd < dpw; ++dd) {
+                DirConst &d = sm.dc[warp][dd];
+                // tau = q + (1 - cos th) z - n_x x - n_y y   (double-float)
+                df tau = df{r0.x, r0.y};
+                tau = df_add(tau, df_mul(df{d.dc_h, d.dc_l}, df{r1.z, r1.w}));
+                const df nx = df_mul(df{d.dsx_h, d.dsx_l}, df{r0.z, r0.w});
+                const df ny = df_mul(df{d.dsy_h, d.dsy_l}, df{r1.x, r1.y});
+                tau = df_add(tau, df{-nx.hi, -nx.lo});
+                tau = df_add(tau, df{-ny.hi, -ny.lo});
+                // previous step's tau (lane 0: carried; the track's first step
+                // compares with a zero phase, synchrad/kernel_farfield.cl:49)
+                float ph = __shfl_up_sync(0xffffffffu, tau.hi, 1);
+                float pl = __shfl_up_sync(0xffffffffu, tau.lo, 1);
+                if (lane == 0) { ph = d.tprev_h; pl = d.tprev_l; }
+                const float dtau = first ? (tau.hi + tau.lo) : ((tau.hi - ph) + (tau.lo - pl));
+                // amplitude on theta-hat / phi-hat
+                const float D = r2.w + d.f_c * r2.z - d.f_sx * r2.x - d.f_sy * r2.y;
+                const float c2 = __frcp_rn(D);
+                const float an = d.f_sx * r3.x + d.f_sy * r3.y + d.f_cz * r3.z;
+                const float c1 = an * c2 * c2;
+                const float tb = d.thx * r2.x + d.thy * r2.y + d.thz * r2.z;
+                const float ta = d.thx * r3.x + d.thy * r3.y + d.thz * r3.z;
+                const float pb = d.phx * r2.x + d.phy * r2.y;
+                const float pa = d.phx * r3.x + d.phy * r3.y;
+                const float amp_t = -(c1 * tb + c2 * ta);
+                const float amp_p = -(c1 * pb + c2 * pa);
+                // rotation between neighbouring omega points, its square, and
+                // its power K/2 (start of the second chain)
+                const df rp = df_mul_raw(d_dw, tau);
+                const float rr = reduce_2pi(rp.hi, rp.lo);
+                float Rs, Rc;
+                sincosf(rr, &Rs, &Rc);
+                float R2c, R2s;
+                cmul(Rc, Rs, Rc, Rs, R2c, R2s);
+                float Hc = 1.f, Hs = 0.f, Pc = Rc, Ps = Rs;
+#pragma unroll
+                for (int e = K / 2; e > 0; e >>= 1) {
+                  if (e & 1) cmul(Hc, Hs, Pc, Ps, Hc, Hs);
+                  cmul(Pc, Ps, Pc, Ps, Pc, Ps);
+                }
+                float4 *st = setup + ((size_t)lane * dpw + dd) * 3;
+                st[0] = make_float4(tau.hi, tau.lo, amp_t, amp_p);
+                st[1] = make_float4(Rc, Rs, R2c, R2s);
+                st[2] = make_float4(Hc, Hs, fabsf(dtau), 0.f);
+                const float th_last = __shfl_sync(0xffffffffu, tau.hi, mcnt - 1);
+                const float tl_last = __shfl_sync(0xffffffffu, tau.lo, mcnt - 1);
+                __syncwarp();
+                if (lane == 0) { d.tprev_h = th_last; d.tprev_l = tl_last; }
+              }
             }
             __syncwarp();
-            // ---- the points: K per lane, two at a time ----
+            // ---- the points: K per lane as two packed rotation chains ----
             for (uint32_t i = 0; i < mcnt; ++i) {
-              const float4 A = sm.setup[warp][i][0];
-              const float4 B = sm.setup[warp][i][1];
-              const float adt = sm.setup[warp][i][2].x;
+              const float4 *st = setup + ((size_t)i * dpw + dsub) * 3;
+              const float4 A = st[0];
+              const float4 B = st[1];
+              const float4 C = st[2];
+              const float adt = C.z;
               const uint32_t s = s0 + c0 + i;
+              float zs, zc;
+              phasor_rev(d_w0.hi, d_w0.lo, A.x, A.y, zs, zc);
               const bool all_in = wabs_max * adt < kPiLo;
               const bool all_out = wabs_min * adt > kPiHi;
               if (uniform && all_in) {
-                const df pz = df_mul_raw(d_w0, df{A.x, A.y});
-                const float r = reduce_2pi(pz.hi, pz.lo);
-                float zs, zc;
-                __sincosf(r, &zs, &zc);
-                float2 Zr = make_float2(zc, zc * B.x - zs * B.y);
-                float2 Zi = make_float2(zs, zc * B.y + zs * B.x);
+                // Fast path: every point of the lane is included and the
+                // omega axis is uniform: two straight-line packed chains.
                 const float2 at = make_float2(A.z, A.z), ap = make_float2(A.w, A.w);
-                const float2 r2c = make_float2(B.z, B.z), r2s = make_float2(B.w, B.w);
-                const float2 nr2s = make_float2(-B.w, -B.w);
+                float2 ZrA = make_float2(zc, zc * B.x - zs * B.y);
+                float2 ZiA = make_float2(zs, zc * B.y + zs * B.x);
+                float2 ZrB, ZiB;
+                rot2(ZrA, ZiA, C.x, C.y, ZrB, ZiB);
 #pragma unroll
-                for (int q = 0; q < KP; ++q) {
-                  aTr[q] = __ffma2_rn(Zr, at, aTr[q]);
-                  aTi[q] = __ffma2_rn(Zi, at, aTi[q]);
-                  aPr[q] = __ffma2_rn(Zr, ap, aPr[q]);
-                  aPi[q] = __ffma2_rn(Zi, ap, aPi[q]);
-                  if (q + 1 < KP) {
-                    const float2 u = __fmul2_rn(Zi, nr2s);
-                    const float2 v = __fmul2_rn(Zr, r2s);
-                    Zr = __ffma2_rn(Zr, r2c, u);
-                    Zi = __ffma2_rn(Zi, r2c, v);
+                for (int q = 0; q < HP; ++q) {
+                  aTr[q] = __ffma2_rn(ZrA, at, aTr[q]);
+                  aTi[q] = __ffma2_rn(ZiA, at, aTi[q]);
+                  aPr[q] = __ffma2_rn(ZrA, ap, aPr[q]);
+                  aPi[q] = __ffma2_rn(ZiA, ap, aPi[q]);
+                  aTr[HP + q] = __ffma2_rn(ZrB, at, aTr[HP + q]);
+                  aTi[HP + q] = __ffma2_rn(ZiB, at, aTi[HP + q]);
+                  aPr[HP + q] = __ffma2_rn(ZrB, ap, aPr[HP + q]);
+                  aPi[HP + q] = __ffma2_rn(ZiB, ap, aPi[HP + q]);
+                  if (q + 1 < HP) {
+                    rot2(ZrA, ZiA, B.z, B.w, ZrA, ZiA);
+                    rot2(ZrB, ZiB, B.z, B.w, ZrB, ZiB);
                   }
                 }
               } else if (!all_out) {
-                // Slow path: per-point mask and/or non-uniform omega.
-                uint32_t mask = 0;
-                for (int m = 0; m < nv; ++m) {
-                  const float2 wd = sm.omega_df[warp][lane * K + m];
-                  const float ph = fabsf(wd.x) * adt;
-                  bool inc;
-                  if (ph < kPiLo) inc = true;
-                  else if (ph > kPiHi) inc = false;
-                  else inc = exact_mask(p, base, s, it_start, p.omega[j0 + m], n0d, n1d, n2d);
-                  mask |= (uint32_t)inc << m;
-                }
-                float zc = 1.f, zs = 0.f;
-#pragma unroll
-                for (int m = 0; m < K; ++m) {
-                  if (!uniform || m == 0) {
-                    const float2 wd = sm.omega_df[warp][lane * K + m];
-                    const df pz = df_mul_raw(df{wd.x, wd.y}, df{A.x, A.y});
-                    const float r = reduce_2pi(pz.hi, pz.lo);
-                    __sincosf(r, &zs, &zc);
-                  } else {
-                    const float nc = zc * B.x - zs * B.y;
-                    zs = zc * B.y + zs * B.x;
-                    zc = nc;
+                // Per-point inclusion only for steps whose phase advance
+                // straddles pi inside this lane's omega range (rare).
+                uint32_t mask = 0xffffffffu;
+                if (!all_in) {
+                  const DirConst &d = sm.dc[warp][dsub];
+                  mask = 0;
+#pragma unroll 1
+                  for (int m = 0; m < nv; ++m) {
+                    const double wm = p.omega[j0 + m];
+                    const float ph = (float)fabs(wm) * adt;
+                    bool inc;
+                    if (ph < kPiLo) inc = true;
+                    else if (ph > kPiHi) inc = false;
+                    else inc = exact_mask(p, base, s, it_start, wm, d.n0, d.n1, d.cT);
+                    mask |= (uint32_t)inc << m;
                   }
-                  if ((mask >> m) & 1u) {
-                    const int q = m >> 1;
-                    if (m & 1) {
-                      aTr[q].y = __fmaf_rn(zc, A.z, aTr[q].y);
-                      aTi[q].y = __fmaf_rn(zs, A.z, aTi[q].y);
-                      aPr[q].y = __fmaf_rn(zc, A.w, aPr[q].y);
-                      aPi[q].y = __fmaf_rn(zs, A.w, aPi[q].y);
-                    } else {
-                      aTr[q].x = __fmaf_rn(zc, A.z, aTr[q].x);
-                      aTi[q].x = __fmaf_rn(zs, A.z, aTi[q].x);
-                      aPr[q].x = __fmaf_rn(zc, A.w, aPr[q].x);
-                      aPi[q].x = __fmaf_rn(zs, A.w, aPi[q].x);
+                }
+                // Phasors of the lane's points: two packed rotation chains
+                // from the reseeded first point (or, for a non-uniform omega
+                // axis, a reseed per point), accumulated as they are formed.
+                float2 ZrA = make_float2(zc, zc * B.x - zs * B.y);
+                float2 ZiA = make_float2(zs, zc * B.y + zs * B.x);
+                float2 ZrB, ZiB;
+                rot2(ZrA, ZiA, C.x, C.y, ZrB, ZiB);
+#pragma unroll
+                for (int q = 0; q < HP; ++q) {
+                  if (!uniform) {
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+#pragma unroll
+                      for (int e = 0; e < 2; ++e) {
+                        const int m = h * (K / 2) + 2 * q + e;
+                        const df wr = df_from_double(p.omega[j0 + min(m, max(nv - 1, 0))] * inv2pi);
+                        float ss, cc;
+                        phasor_rev(wr.hi, wr.lo, A.x, A.y, ss, cc);
+                        if (h == 0) {
+                          if (e == 0) { ZrA.x = cc; ZiA.x = ss; } else { ZrA.y = cc; ZiA.y = ss; }
+                        } else {
+                          if (e == 0) { ZrB.x = cc; ZiB.x = ss; } else { ZrB.y = cc; ZiB.y = ss; }
+                        }
+                      }
                     }
+                  }
+                  float2 atA = make_float2(A.z, A.z), apA = make_float2(A.w, A.w);
+                  float2 atB = atA, apB = apA;
+                  if (!all_in) {
+                    const int mA = 2 * q, mB = K / 2 + 2 * q;
+                    const float a0 = (mask >> mA) & 1u ? 1.f : 0.f, a1 = (mask >> (mA + 1)) & 1u ? 1.f : 0.f;
+                    const float b0 = (mask >> mB) & 1u ? 1.f : 0.f, b1 = (mask >> (mB + 1)) & 1u ? 1.f : 0.f;
+                    atA = make_float2(A.z * a0, A.z * a1); apA = make_float2(A.w * a0, A.w * a1);
+                    atB = make_float2(A.z * b0, A.z * b1); apB = make_float2(A.w * b0, A.w * b1);
+                  }
+                  aTr[q] = __ffma2_rn(ZrA, atA, aTr[q]);
+                  aTi[q] = __ffma2_rn(ZiA, atA, aTi[q]);
+                  aPr[q] = __ffma2_rn(ZrA, apA, aPr[q]);
+                  aPi[q] = __ffma2_rn(ZiA, apA, aPi[q]);
+                  aTr[HP + q] = __ffma2_rn(ZrB, atB, aTr[HP + q]);
+                  aTi[HP + q] = __ffma2_rn(ZiB, atB, aTi[HP + q]);
+                  aPr[HP + q] = __ffma2_rn(ZrB, apB, aPr[HP + q]);
+                  aPi[HP + q] = __ffma2_rn(ZiB, apB, aPi[HP + q]);
+                  if (q + 1 < HP && uniform) {
+                    rot2(ZrA, ZiA, B.z, B.w, ZrA, ZiA);
+                    rot2(ZrB, ZiB, B.z, B.w, ZrB, ZiB);
                   }
                 }
               }
@@ -490,25 +603,8 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
             }
             __syncwarp();
           }
-          // ---- fold the stage's FP32 sums into the compensated pairs ----
-#pragma unroll
-          for (int m = 0; m < K; ++m) {
-            const int q = m >> 1;
-            const float v[4] = {(m & 1) ? aTr[q].y : aTr[q].x, (m & 1) ? aTi[q].y : aTi[q].x,
-                                (m & 1) ? aPr[q].y : aPr[q].x, (m & 1) ? aPi[q].y : aPi[q].x};
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-              float &S = sm.kahan[warp][m][c][lane];
-              float &C = sm.kahan[warp][m][c + 4][lane];
-              const df e = two_sum(S, v[c]);
-              S = e.hi;
-              C += e.lo;
-            }
-          }
-#pragma unroll
-          for (int q = 0; q < KP; ++q) {
-            aTr[q] = aTi[q] = aPr[q] = aPi[q] = make_float2(0.f, 0.f);
-          }
+          // ---- fold the FP32 sums into the compensated pairs every few stages ----
+          if ((stage_in_track + 1) % kFoldStages == 0) fold();
         } else {
           // inactive warp: keep the snapshot state in step with the others
           for (uint32_t i = 0; i < cnt; ++i) {
@@ -524,8 +620,11 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
         flush(snap.k);
         snap.advance(it_start, it_end, snaps, p.n_snaps);
       }
+      // the next track starts with empty carried tau
+      if (ll == 0) { sm.dc[warp][dsub].tprev_h = 0.f; sm.dc[warp][dsub].tprev_l = 0.f; }
+      __syncwarp();
     }
-    (void)pending;
+    __syncwarp();
   }
 }
 
@@ -544,83 +643,69 @@ __global__ void far_reduce_kernel(FarMixedParams p) {
   }
 }
 
-template <int K, int W>
+constexpr int kW = 8;  // warps per CTA
+
+size_t smem_bytes(int dpw) {
+  return sizeof(SmemFixed<kW>) + (size_t)kW * 32 * dpw * 3 * sizeof(float4);
+}
+
+template <int K>
 int launch_main(const FarMixedParams &p, int grid, cudaStream_t s) {
-  const size_t smem = sizeof(Smem<K, W>);
-  cudaError_t e = cudaFuncSetAttribute(far_mixed_kernel<K, W>,
+  const size_t smem = smem_bytes((int)p.dpw);
+  cudaError_t e = cudaFuncSetAttribute(far_mixed_kernel<K, kW>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_fail(e, "far_mixed smem attribute");
-  far_mixed_kernel<K, W><<<grid, W * 32, smem, s>>>(p);
+  far_mixed_kernel<K, kW><<<grid, kW * 32, smem, s>>>(p);
   return cuda_fail(cudaGetLastError(), "far_mixed kernel launch");
 }
 
-template <int W>
 int dispatch_k(int K, const FarMixedParams &p, int grid, cudaStream_t s) {
   switch (K) {
-    case 2: return launch_main<2, W>(p, grid, s);
-    case 4: return launch_main<4, W>(p, grid, s);
-    case 6: return launch_main<6, W>(p, grid, s);
-    case 8: return launch_main<8, W>(p, grid, s);
-    case 10: return launch_main<10, W>(p, grid, s);
-    case 12: return launch_main<12, W>(p, grid, s);
-    case 14: return launch_main<14, W>(p, grid, s);
-    case 16: return launch_main<16, W>(p, grid, s);
+    case 8: return launch_main<8>(p, grid, s);
+    case 16: return launch_main<16>(p, grid, s);
+    case 24: return launch_main<24>(p, grid, s);
+    case 32: return launch_main<32>(p, grid, s);
     default: return fail(SR_ERR_INVALID, "unsupported points per lane %d", K);
-  }
-}
-
-template <int K, int W>
-int occupancy_of() {
-  int n = 0;
-  const size_t smem = sizeof(Smem<K, W>);
-  cudaFuncSetAttribute(far_mixed_kernel<K, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)smem);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, far_mixed_kernel<K, W>, W * 32, smem) !=
-      cudaSuccess)
-    n = 1;
-  return n > 0 ? n : 1;
-}
-
-int occupancy(int K, int W) {
-  if (W != 8) return 1;
-  switch (K) {
-    case 2: return occupancy_of<2, 8>();
-    case 4: return occupancy_of<4, 8>();
-    case 6: return occupancy_of<6, 8>();
-    case 8: return occupancy_of<8, 8>();
-    case 10: return occupancy_of<10, 8>();
-    case 12: return occupancy_of<12, 8>();
-    case 14: return occupancy_of<14, 8>();
-    default: return occupancy_of<16, 8>();
   }
 }
 
 }  // namespace
 
+// Work shape: K points per lane and L lanes per direction (32/L directions per
+// warp).  The widest lane chunk (K = 32) amortises the per-step reseed best;
+// narrower omega axes put several directions in one warp.
 FarMixedConfig far_mixed_choose(uint32_t n_omega, uint32_t n_dirs, uint32_t n_tracks,
                                 int n_sm) {
   FarMixedConfig c;
-  int k = (int)((n_omega + 31) / 32);
-  k += k & 1;
-  c.K = k < 2 ? 2 : (k > 16 ? 16 : k);
-  c.W = 8;
+  c.W = kW;
   c.ctas_per_sm = 1;
-  const uint64_t n_wtiles = (n_omega + 32u * c.K - 1) / (32u * c.K);
-  const uint64_t groups = (n_dirs * n_wtiles + c.W - 1) / c.W;
+  c.K = 32;
+  int L = 32;
+  while (L > 32 / kMaxDpw && (uint32_t)(L / 2) * 32u >= n_omega) L /= 2;
+  // narrow axes: shrink K while the lanes of a direction would idle
+  while (c.K > 8 && (uint32_t)(L * (c.K - 8)) >= n_omega) c.K -= 8;
+  c.L = L;
+  c.dpw = 32 / L;
+  const uint64_t n_wtiles = (n_omega + (uint64_t)L * c.K - 1) / ((uint64_t)L * c.K);
+  const uint64_t dgroups = (n_dirs + c.dpw - 1) / c.dpw;
+  const uint64_t groups = (dgroups * n_wtiles + c.W - 1) / c.W;
   const uint64_t capacity = (uint64_t)n_sm * c.ctas_per_sm;
   uint64_t nsub = (16 * capacity + groups - 1) / (groups ? groups : 1);
   if (nsub > n_tracks) nsub = n_tracks;
   if (nsub < 1) nsub = 1;
   if (nsub > 64) nsub = 64;
   c.n_sub = (int)nsub;
+  c.grid = (int)std::min<uint64_t>(groups * nsub, capacity);
+  if (c.grid < 1) c.grid = 1;
   return c;
 }
 
 size_t far_mixed_workspace(int64_t total_steps, uint64_t n_points, int n_out, uint32_t n_snaps,
                            const FarMixedConfig &cfg) {
-  size_t b = 256;                                          // status word
-  b += ((size_t)total_steps * 64 + 255) / 256 * 256;       // step records
-  b += (size_t)cfg.n_sub * n_out * n_snaps * n_points * 8; // partial spectra
+  size_t b = 256;                                                    // status word
+  b += ((size_t)total_steps * 64 + 255) / 256 * 256;                 // step records
+  b += ((size_t)cfg.n_sub * n_out * n_snaps * n_points * 8 + 255) / 256 * 256;  // partials
+  b += (size_t)cfg.grid * cfg.W * cfg.K * 8 * 32 * sizeof(float);   // compensated sums
   return b;
 }
 
@@ -633,12 +718,18 @@ int launch_far_mixed(FarMixedParams p, const FarMixedConfig &cfg, void *ws, size
     return fail(SR_ERR_WORKSPACE, "workspace of %zu bytes needed, %zu given", need, ws_bytes);
   if (((uintptr_t)ws & 255u) != 0) return fail(SR_ERR_WORKSPACE, "workspace not 256-byte aligned");
   unsigned char *w = (unsigned char *)ws;
+  size_t off = 256;
   p.status = (int *)w;
-  p.records = (float4 *)(w + 256);
-  p.partial = (double *)(w + 256 + ((size_t)p.total_steps * 64 + 255) / 256 * 256);
-  p.n_wtiles = (p.n_omega + 32u * cfg.K - 1) / (32u * cfg.K);
+  p.records = (float4 *)(w + off);
+  off += ((size_t)p.total_steps * 64 + 255) / 256 * 256;
+  p.partial = (double *)(w + off);
+  off += ((size_t)cfg.n_sub * p.n_out * p.n_snaps * P * 8 + 255) / 256 * 256;
+  p.outer = (float *)(w + off);
+  p.dpw = (uint32_t)cfg.dpw;
+  p.n_wtiles = (p.n_omega + (uint32_t)(cfg.L * cfg.K) - 1) / (uint32_t)(cfg.L * cfg.K);
   const uint32_t n_dirs = p.n_theta * p.n_phi;
-  p.n_groups = (uint32_t)(((uint64_t)n_dirs * p.n_wtiles + cfg.W - 1) / cfg.W);
+  const uint32_t dgroups = (n_dirs + cfg.dpw - 1) / cfg.dpw;
+  p.n_groups = (uint32_t)(((uint64_t)dgroups * p.n_wtiles + cfg.W - 1) / cfg.W);
   p.n_sub = (uint32_t)cfg.n_sub;
   p.n_items = p.n_groups * p.n_sub;
 
@@ -661,12 +752,9 @@ int launch_far_mixed(FarMixedParams p, const FarMixedConfig &cfg, void *ws, size
     int rc = cuda_fail(cudaGetLastError(), "far prepass launch");
     if (rc) return rc;
   }
-  const int occ = occupancy(cfg.K, cfg.W);
-  int grid = n_sm * occ;
-  if ((uint32_t)grid > p.n_items) grid = (int)p.n_items;
   void *tok = nullptr;
   timing_record(stream, true, &tok);
-  int rc = dispatch_k<8>(cfg.K, p, grid, stream);
+  int rc = dispatch_k(cfg.K, p, cfg.grid, stream);
   timing_record(stream, false, &tok);
   if (rc) return rc;
   const uint64_t total = (uint64_t)p.n_out * p.n_snaps * P;

@@ -55,9 +55,11 @@ struct FarMixedParams {
   uint32_t n_groups;   // CTA-sized groups of warp tasks
   uint32_t n_sub;      // track subsets
   uint32_t n_items;    // n_groups * n_sub
+  uint32_t dpw;        // directions per warp
   // workspace
   float4 *records;     // [total_steps][4]
   double *partial;     // [n_sub][n_out][n_snaps][P]
+  float *outer;        // [grid][W][K][8][32] compensated per-track sums
   int *status;
   // outputs
   double *out[6];
@@ -66,8 +68,11 @@ struct FarMixedParams {
 struct FarMixedConfig {
   int K;        // points per lane
   int W;        // warps per CTA
+  int L;        // lanes per direction
+  int dpw;      // directions per warp (32 / L)
   int n_sub;    // track subsets
   int ctas_per_sm;
+  int grid;     // CTAs of the persistent launch
 };
 
 FarMixedConfig far_mixed_choose(uint32_t n_omega, uint32_t n_dirs,
