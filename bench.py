@@ -274,7 +274,7 @@ def main():
     roofline = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak if peak else None,
                 "traffic": None,
-                "kernel": "far_mixed_kernel<16,8>",
+                "kernel": "far_mixed_kernel (32 omega points per lane, 8 warps per CTA)",
                 "kernel_ms_avg": kern_avg_ms,
                 "flops_per_unit": FLOPS_PER_UNIT,
                 "frac_canonical_18_flops": (achieved * CANONICAL_FLOPS / FLOPS_PER_UNIT / peak

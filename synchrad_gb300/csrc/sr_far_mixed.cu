@@ -164,10 +164,10 @@ struct DirConst {
   float f_c, f_sx, f_sy, f_cz;                   // the same in FP32
   float thx, thy, thz, phx, phy;                 // theta-hat, phi-hat
   float tprev_h, tprev_l;                        // tau of the step before the current chunk
-  float pad_;
+  float adt_max;                                 // largest |dtau| of the current chunk
 };
 
-constexpr int kMaxDpw = 8;  // directions per warp (omega tiles narrower than 32 lanes)
+constexpr int kMaxDpw = 4;  // directions per warp (omega tiles narrower than 32 lanes)
 
 template <int W>
 struct SmemFixed {
@@ -175,7 +175,7 @@ struct SmemFixed {
   uint64_t bar[2];
   uint64_t pad_[2];
   DirConst dc[W][kMaxDpw];
-  // followed by float4 setup[W][32][dpw][3]
+  // followed by float4 setup[W][32][dpw][6]
 };
 
 // exp(i 2 pi w tau) for a double-float frequency in revolutions: the phase is
@@ -201,6 +201,15 @@ __device__ __forceinline__ void rot2(float2 zr, float2 zi, float rc, float rs, f
   oi = __ffma2_rn(zi, make_float2(rc, rc), v);
 }
 
+// (zr + i zi) * (rc + i rs) for two points at once, factors given as pairs.
+__device__ __forceinline__ void rot2p(float2 zr, float2 zi, float2 rc, float2 rs, float2 nrs,
+                                      float2 &or_, float2 &oi) {
+  const float2 u = __fmul2_rn(zi, nrs);
+  const float2 v = __fmul2_rn(zr, rs);
+  or_ = __ffma2_rn(zr, rc, u);
+  oi = __ffma2_rn(zi, rc, v);
+}
+
 __device__ __forceinline__ void cmul(float ar, float ai, float br, float bi, float &cr,
                                      float &ci) {
   cr = ar * br - ai * bi;
@@ -218,7 +227,7 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
   float4 *setup_all = reinterpret_cast<float4 *>(smem_raw + sizeof(SmemFixed<W>));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int dsub = lane / L, ll = lane % L;
-  float4 *setup = setup_all + (size_t)warp * 32 * dpw * 3;
+  float4 *setup = setup_all + (size_t)warp * 32 * dpw * 6;
   constexpr int KP = K / 2, HP = KP / 2;
 
   if (threadIdx.x == 0) {
@@ -483,122 +492,146 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
                   if (e & 1) cmul(Hc, Hs, Pc, Ps, Hc, Hs);
                   cmul(Pc, Ps, Pc, Ps, Pc, Ps);
                 }
-                float4 *st = setup + ((size_t)lane * dpw + dd) * 3;
-                st[0] = make_float4(tau.hi, tau.lo, amp_t, amp_p);
-                st[1] = make_float4(Rc, Rs, R2c, R2s);
-                st[2] = make_float4(Hc, Hs, fabsf(dtau), 0.f);
+                float4 *st = setup + ((size_t)lane * dpw + dd) * 6;
+                st[0] = make_float4(tau.hi, tau.lo, Rc, Rs);
+                st[1] = make_float4(amp_t, amp_t, amp_p, amp_p);
+                st[2] = make_float4(R2c, R2c, R2s, R2s);
+                st[3] = make_float4(-R2s, -R2s, Hc, Hc);
+                st[4] = make_float4(Hs, Hs, -Hs, -Hs);
+                st[5] = make_float4(fabsf(dtau), 0.f, 0.f, 0.f);
+                // largest |dtau| of the chunk: decides the chunk's fast loop
+                const float am = (uint32_t)lane < mcnt ? fabsf(dtau) : 0.f;
+                const float amax = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(am)));
                 const float th_last = __shfl_sync(0xffffffffu, tau.hi, mcnt - 1);
                 const float tl_last = __shfl_sync(0xffffffffu, tau.lo, mcnt - 1);
                 __syncwarp();
-                if (lane == 0) { d.tprev_h = th_last; d.tprev_l = tl_last; }
+                if (lane == 0) { d.tprev_h = th_last; d.tprev_l = tl_last; d.adt_max = amax; }
               }
             }
             __syncwarp();
             // ---- the points: K per lane as two packed rotation chains ----
-            for (uint32_t i = 0; i < mcnt; ++i) {
-              const float4 *st = setup + ((size_t)i * dpw + dsub) * 3;
-              const float4 A = st[0];
-              const float4 B = st[1];
-              const float4 C = st[2];
-              const float adt = C.z;
-              const uint32_t s = s0 + c0 + i;
+            // A chunk whose steps are all included for this lane's omega range,
+            // with a uniform axis and no snapshot write, runs the tight loop.
+            const bool fire_here = snap.fire_it >= (int64_t)(s0 + c0) &&
+                                   snap.fire_it < (int64_t)(s0 + c0 + mcnt);
+            // One fully included step on a uniform axis: two packed chains.
+            auto step_fast = [&](const float4 *st) {
+              const float4 A = st[0], AT = st[1], R2 = st[2], X = st[3], Y = st[4];
               float zs, zc;
               phasor_rev(d_w0.hi, d_w0.lo, A.x, A.y, zs, zc);
-              const bool all_in = wabs_max * adt < kPiLo;
-              const bool all_out = wabs_min * adt > kPiHi;
-              if (uniform && all_in) {
-                // Fast path: every point of the lane is included and the
-                // omega axis is uniform: two straight-line packed chains.
-                const float2 at = make_float2(A.z, A.z), ap = make_float2(A.w, A.w);
-                float2 ZrA = make_float2(zc, zc * B.x - zs * B.y);
-                float2 ZiA = make_float2(zs, zc * B.y + zs * B.x);
-                float2 ZrB, ZiB;
-                rot2(ZrA, ZiA, C.x, C.y, ZrB, ZiB);
+              const float2 at = make_float2(AT.x, AT.y), ap = make_float2(AT.z, AT.w);
+              const float2 r2c = make_float2(R2.x, R2.y), r2s = make_float2(R2.z, R2.w);
+              const float2 nr2s = make_float2(X.x, X.y), hc = make_float2(X.z, X.w);
+              const float2 hs = make_float2(Y.x, Y.y), nhs = make_float2(Y.z, Y.w);
+              float2 ZrA = make_float2(zc, zc * A.z - zs * A.w);
+              float2 ZiA = make_float2(zs, zc * A.w + zs * A.z);
+              float2 ZrB, ZiB;
+              rot2p(ZrA, ZiA, hc, hs, nhs, ZrB, ZiB);
 #pragma unroll
-                for (int q = 0; q < HP; ++q) {
-                  aTr[q] = __ffma2_rn(ZrA, at, aTr[q]);
-                  aTi[q] = __ffma2_rn(ZiA, at, aTi[q]);
-                  aPr[q] = __ffma2_rn(ZrA, ap, aPr[q]);
-                  aPi[q] = __ffma2_rn(ZiA, ap, aPi[q]);
-                  aTr[HP + q] = __ffma2_rn(ZrB, at, aTr[HP + q]);
-                  aTi[HP + q] = __ffma2_rn(ZiB, at, aTi[HP + q]);
-                  aPr[HP + q] = __ffma2_rn(ZrB, ap, aPr[HP + q]);
-                  aPi[HP + q] = __ffma2_rn(ZiB, ap, aPi[HP + q]);
-                  if (q + 1 < HP) {
-                    rot2(ZrA, ZiA, B.z, B.w, ZrA, ZiA);
-                    rot2(ZrB, ZiB, B.z, B.w, ZrB, ZiB);
-                  }
+              for (int q = 0; q < HP; ++q) {
+                aTr[q] = __ffma2_rn(ZrA, at, aTr[q]);
+                aTi[q] = __ffma2_rn(ZiA, at, aTi[q]);
+                aPr[q] = __ffma2_rn(ZrA, ap, aPr[q]);
+                aPi[q] = __ffma2_rn(ZiA, ap, aPi[q]);
+                aTr[HP + q] = __ffma2_rn(ZrB, at, aTr[HP + q]);
+                aTi[HP + q] = __ffma2_rn(ZiB, at, aTi[HP + q]);
+                aPr[HP + q] = __ffma2_rn(ZrB, ap, aPr[HP + q]);
+                aPi[HP + q] = __ffma2_rn(ZiB, ap, aPi[HP + q]);
+                if (q + 1 < HP) {
+                  rot2p(ZrA, ZiA, r2c, r2s, nr2s, ZrA, ZiA);
+                  rot2p(ZrB, ZiB, r2c, r2s, nr2s, ZrB, ZiB);
                 }
-              } else if (!all_out) {
-                // Per-point inclusion only for steps whose phase advance
-                // straddles pi inside this lane's omega range (rare).
-                uint32_t mask = 0xffffffffu;
-                if (!all_in) {
-                  const DirConst &d = sm.dc[warp][dsub];
-                  mask = 0;
+              }
+            };
+            if (uniform && !fire_here && wabs_max * sm.dc[warp][dsub].adt_max < kPiLo) {
+              const float4 *st = setup + (size_t)dsub * 6;
+              const size_t stride = (size_t)dpw * 6;
+              for (uint32_t i = 0; i < mcnt; ++i, st += stride) step_fast(st);
+            } else {
+              // General loop: per-step decision, per-point mask where the
+              // phase advance straddles pi, non-uniform omega, snapshot writes.
 #pragma unroll 1
-                  for (int m = 0; m < nv; ++m) {
-                    const double wm = p.omega[j0 + m];
-                    const float ph = (float)fabs(wm) * adt;
-                    bool inc;
-                    if (ph < kPiLo) inc = true;
-                    else if (ph > kPiHi) inc = false;
-                    else inc = exact_mask(p, base, s, it_start, wm, d.n0, d.n1, d.cT);
-                    mask |= (uint32_t)inc << m;
+              for (uint32_t i = 0; i < mcnt; ++i) {
+                const float4 *st = setup + ((size_t)i * dpw + dsub) * 6;
+                const float adt = st[5].x;
+                const uint32_t s = s0 + c0 + i;
+                const bool all_in = wabs_max * adt < kPiLo;
+                const bool all_out = wabs_min * adt > kPiHi;
+                if (uniform && all_in) {
+                  step_fast(st);
+                } else if (!all_out && nv > 0) {
+                  const float4 A = st[0], AT = st[1], R2 = st[2], X = st[3], Y = st[4];
+                  uint32_t mask = 0xffffffffu;
+                  if (!all_in) {
+                    const DirConst &d = sm.dc[warp][dsub];
+                    mask = 0;
+#pragma unroll 1
+                    for (int m = 0; m < nv; ++m) {
+                      const double wm = p.omega[j0 + m];
+                      const float ph = (float)fabs(wm) * adt;
+                      bool inc;
+                      if (ph < kPiLo) inc = true;
+                      else if (ph > kPiHi) inc = false;
+                      else inc = exact_mask(p, base, s, it_start, wm, d.n0, d.n1, d.cT);
+                      mask |= (uint32_t)inc << m;
+                    }
                   }
-                }
-                // Phasors of the lane's points: two packed rotation chains
-                // from the reseeded first point (or, for a non-uniform omega
-                // axis, a reseed per point), accumulated as they are formed.
-                float2 ZrA = make_float2(zc, zc * B.x - zs * B.y);
-                float2 ZiA = make_float2(zs, zc * B.y + zs * B.x);
-                float2 ZrB, ZiB;
-                rot2(ZrA, ZiA, C.x, C.y, ZrB, ZiB);
+                  float zs, zc;
+                  phasor_rev(d_w0.hi, d_w0.lo, A.x, A.y, zs, zc);
+                  // phasors as two packed chains from the reseeded first point
+                  // (uniform axis) or one reseed per point (non-uniform axis);
+                  // amplitudes zeroed per point where the step is masked out
+                  float2 ZrA = make_float2(zc, zc * A.z - zs * A.w);
+                  float2 ZiA = make_float2(zs, zc * A.w + zs * A.z);
+                  float2 ZrB, ZiB;
+                  rot2p(ZrA, ZiA, make_float2(X.z, X.w), make_float2(Y.x, Y.y),
+                        make_float2(Y.z, Y.w), ZrB, ZiB);
 #pragma unroll
-                for (int q = 0; q < HP; ++q) {
-                  if (!uniform) {
+                  for (int q = 0; q < HP; ++q) {
+                    if (!uniform) {
 #pragma unroll
-                    for (int h = 0; h < 2; ++h) {
+                      for (int h = 0; h < 2; ++h) {
 #pragma unroll
-                      for (int e = 0; e < 2; ++e) {
-                        const int m = h * (K / 2) + 2 * q + e;
-                        const df wr = df_from_double(p.omega[j0 + min(m, max(nv - 1, 0))] * inv2pi);
-                        float ss, cc;
-                        phasor_rev(wr.hi, wr.lo, A.x, A.y, ss, cc);
-                        if (h == 0) {
-                          if (e == 0) { ZrA.x = cc; ZiA.x = ss; } else { ZrA.y = cc; ZiA.y = ss; }
-                        } else {
-                          if (e == 0) { ZrB.x = cc; ZiB.x = ss; } else { ZrB.y = cc; ZiB.y = ss; }
+                        for (int e = 0; e < 2; ++e) {
+                          const int m = h * (K / 2) + 2 * q + e;
+                          const df wr = df_from_double(p.omega[j0 + min(m, nv - 1)] * inv2pi);
+                          float ss, cc;
+                          phasor_rev(wr.hi, wr.lo, A.x, A.y, ss, cc);
+                          float2 &zr = h ? ZrB : ZrA;
+                          float2 &zi = h ? ZiB : ZiA;
+                          if (e == 0) { zr.x = cc; zi.x = ss; } else { zr.y = cc; zi.y = ss; }
                         }
                       }
                     }
-                  }
-                  float2 atA = make_float2(A.z, A.z), apA = make_float2(A.w, A.w);
-                  float2 atB = atA, apB = apA;
-                  if (!all_in) {
                     const int mA = 2 * q, mB = K / 2 + 2 * q;
-                    const float a0 = (mask >> mA) & 1u ? 1.f : 0.f, a1 = (mask >> (mA + 1)) & 1u ? 1.f : 0.f;
-                    const float b0 = (mask >> mB) & 1u ? 1.f : 0.f, b1 = (mask >> (mB + 1)) & 1u ? 1.f : 0.f;
-                    atA = make_float2(A.z * a0, A.z * a1); apA = make_float2(A.w * a0, A.w * a1);
-                    atB = make_float2(A.z * b0, A.z * b1); apB = make_float2(A.w * b0, A.w * b1);
-                  }
-                  aTr[q] = __ffma2_rn(ZrA, atA, aTr[q]);
-                  aTi[q] = __ffma2_rn(ZiA, atA, aTi[q]);
-                  aPr[q] = __ffma2_rn(ZrA, apA, aPr[q]);
-                  aPi[q] = __ffma2_rn(ZiA, apA, aPi[q]);
-                  aTr[HP + q] = __ffma2_rn(ZrB, atB, aTr[HP + q]);
-                  aTi[HP + q] = __ffma2_rn(ZiB, atB, aTi[HP + q]);
-                  aPr[HP + q] = __ffma2_rn(ZrB, apB, aPr[HP + q]);
-                  aPi[HP + q] = __ffma2_rn(ZiB, apB, aPi[HP + q]);
-                  if (q + 1 < HP && uniform) {
-                    rot2(ZrA, ZiA, B.z, B.w, ZrA, ZiA);
-                    rot2(ZrB, ZiB, B.z, B.w, ZrB, ZiB);
+                    const float a0 = ((mask >> mA) & 1u) ? 1.f : 0.f;
+                    const float a1 = ((mask >> (mA + 1)) & 1u) ? 1.f : 0.f;
+                    const float b0 = ((mask >> mB) & 1u) ? 1.f : 0.f;
+                    const float b1 = ((mask >> (mB + 1)) & 1u) ? 1.f : 0.f;
+                    const float2 atA = make_float2(AT.x * a0, AT.x * a1);
+                    const float2 apA = make_float2(AT.z * a0, AT.z * a1);
+                    const float2 atB = make_float2(AT.x * b0, AT.x * b1);
+                    const float2 apB = make_float2(AT.z * b0, AT.z * b1);
+                    aTr[q] = __ffma2_rn(ZrA, atA, aTr[q]);
+                    aTi[q] = __ffma2_rn(ZiA, atA, aTi[q]);
+                    aPr[q] = __ffma2_rn(ZrA, apA, aPr[q]);
+                    aPi[q] = __ffma2_rn(ZiA, apA, aPi[q]);
+                    aTr[HP + q] = __ffma2_rn(ZrB, atB, aTr[HP + q]);
+                    aTi[HP + q] = __ffma2_rn(ZiB, atB, aTi[HP + q]);
+                    aPr[HP + q] = __ffma2_rn(ZrB, apB, aPr[HP + q]);
+                    aPi[HP + q] = __ffma2_rn(ZiB, apB, aPi[HP + q]);
+                    if (q + 1 < HP && uniform) {
+                      rot2p(ZrA, ZiA, make_float2(R2.x, R2.y), make_float2(R2.z, R2.w),
+                            make_float2(X.x, X.y), ZrA, ZiA);
+                      rot2p(ZrB, ZiB, make_float2(R2.x, R2.y), make_float2(R2.z, R2.w),
+                            make_float2(X.x, X.y), ZrB, ZiB);
+                    }
                   }
                 }
-              }
-              if ((int64_t)s == snap.fire_it) {  // uniform over the CTA
-                flush(snap.k);
-                snap.advance(it_start, it_end, snaps, p.n_snaps);
+                if ((int64_t)s == snap.fire_it) {  // uniform over the CTA
+                  flush(snap.k);
+                  snap.advance(it_start, it_end, snaps, p.n_snaps);
+                }
               }
             }
             __syncwarp();
@@ -646,7 +679,7 @@ __global__ void far_reduce_kernel(FarMixedParams p) {
 constexpr int kW = 8;  // warps per CTA
 
 size_t smem_bytes(int dpw) {
-  return sizeof(SmemFixed<kW>) + (size_t)kW * 32 * dpw * 3 * sizeof(float4);
+  return sizeof(SmemFixed<kW>) + (size_t)kW * 32 * dpw * 6 * sizeof(float4);
 }
 
 template <int K>
