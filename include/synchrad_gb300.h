@@ -117,6 +117,19 @@ int sr_spectrum(const sr_tracks *tracks, const sr_grid *grid, int comp,
                 int precision, void *const *out, void *workspace,
                 size_t workspace_bytes, void *stream);
 
+/* The mixed-precision far field of sr_spectrum without any device allocation.
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory themselves (code embedded in a host application that owns every
+ * allocation and hands over only input and output buffers): the scratch lives
+ * in a 64 MiB array compiled into this library, held by every GPU that loads
+ * it until the process exits.  Sizes whose scratch (64 B per track step, 8 B
+ * per point x output x snapshot, plus per-CTA sums) exceeds it are rejected
+ * with SR_ERR_INVALID.  The first call on a device looks up the array's device
+ * address (make it before any stream capture); calls that overlap on the GPU
+ * share the array and race.  Far field only; outputs are double, accumulated. */
+int sr_spectrum_noalloc(const sr_tracks *tracks, const sr_grid *grid, int comp,
+                        void *const *out, void *stream);
+
 /* Scratch bytes sr_spectrum needs for these sizes (reads host fields only). */
 int64_t sr_workspace_bytes(const sr_tracks *tracks, const sr_grid *grid,
                            int comp, int precision);

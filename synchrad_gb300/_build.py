@@ -25,6 +25,7 @@ SOURCES = {
     "sr_port.cu": ["--fmad=false"],
     "sr_far_mixed.cu": [],
     "sr_diag.cu": [],
+    "sr_noalloc.cu": [],
 }
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",

@@ -90,7 +90,7 @@ EXPORTS = (
     "sr_far_cartesian_comps_complex", "sr_far_spheric_comps",
     "sr_far_spheric_comps_complex", "sr_near_total", "sr_near_cartesian_comps",
     "sr_near_cartesian_comps_complex", "sr_timing_enable", "sr_timing_read",
-    "sr_probe_fp32_peak",
+    "sr_probe_fp32_peak", "sr_spectrum_noalloc",
 )
 
 _lock = threading.Lock()
@@ -102,6 +102,9 @@ def _declare(L: ctypes.CDLL) -> None:
     L.sr_spectrum.restype = i32
     L.sr_spectrum.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid), i32, i32,
                               ctypes.POINTER(vp), vp, ctypes.c_size_t, vp]
+    L.sr_spectrum_noalloc.restype = i32
+    L.sr_spectrum_noalloc.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid), i32,
+                                      ctypes.POINTER(vp), vp]
     L.sr_workspace_bytes.restype = ctypes.c_int64
     L.sr_workspace_bytes.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid), i32, i32]
     L.sr_workspace_status.restype = i32

@@ -108,6 +108,19 @@ FarMixedParams far_mixed_params(const sr_tracks *t, const sr_grid *g, int comp,
 }
 
 }  // namespace
+
+// The checks and parameter packing of sr_spectrum, for other entry points of
+// the library that evaluate the same mixed-precision far field.
+int validate_spectrum_args(const sr_tracks *t, const sr_grid *g, int comp, int precision,
+                           void *const *out) {
+  return check_common(t, g, comp, precision, out);
+}
+FarMixedParams make_far_mixed_params(const sr_tracks *t, const sr_grid *g, int comp,
+                                     void *const *out) {
+  return far_mixed_params(t, g, comp, out);
+}
+int device_sm_count() { return n_sm_of_current_device(); }
+
 }  // namespace sr
 
 using namespace sr;

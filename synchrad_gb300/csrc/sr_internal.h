@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/synchrad_gb300.h"
+
 namespace sr {
 
 // Arguments of the plain-port kernels (one thread per spectral point, every
@@ -81,5 +83,12 @@ size_t far_mixed_workspace(int64_t total_steps, uint64_t n_points, int n_out,
                            uint32_t n_snaps, const FarMixedConfig &cfg);
 int launch_far_mixed(FarMixedParams p, const FarMixedConfig &cfg,
                      void *workspace, size_t ws_bytes, cudaStream_t stream);
+
+// sr_api.cu: argument checks and parameter packing shared by entry points.
+int validate_spectrum_args(const sr_tracks *t, const sr_grid *g, int comp,
+                           int precision, void *const *out);
+FarMixedParams make_far_mixed_params(const sr_tracks *t, const sr_grid *g,
+                                     int comp, void *const *out);
+int device_sm_count();
 
 }  // namespace sr
