@@ -50,9 +50,13 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--tracks", type=int, default=1024)
-    ap.add_argument("--track-steps", type=int, default=4000)
-    ap.add_argument("--grid", type=int, nargs=3, default=[512, 64, 64])
+    ap.add_argument("--workload", default="far", choices=["far", "near", "ragged"],
+                    help="far: the headline configuration (default); near: 2048 helical "
+                         "tracks on a screen at 20 undulator lengths; ragged: 8192 FP32 "
+                         "betatron tracks of 500-20000 steps")
+    ap.add_argument("--tracks", type=int, default=None)
+    ap.add_argument("--track-steps", type=int, default=None)
+    ap.add_argument("--grid", type=int, nargs=3, default=None)
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -122,8 +126,26 @@ class ClockSampler:
 
 def make_workload(args):
     from synchrad_gb300 import workloads as wl
-    return wl.c2_far_mixed(n_tracks=args.tracks, n_steps=args.track_steps,
-                           grid=tuple(args.grid))
+    kw = {}
+    if args.tracks is not None:
+        kw["n_tracks"] = args.tracks
+    if args.grid is not None:
+        kw["grid"] = tuple(args.grid)
+    if args.workload == "far":
+        if args.track_steps is not None:
+            kw["n_steps"] = args.track_steps
+        return wl.c2_far_mixed(**kw)
+    if args.workload == "near":
+        if args.track_steps is not None:
+            kw["n_steps"] = args.track_steps
+        return wl.c5_near_helical(**kw)
+    if args.track_steps is not None:
+        kw["steps_range"] = (max(2, args.track_steps // 40), args.track_steps)
+    return wl.c3_betatron_ragged(**kw)
+
+
+def flops_per_unit(w):
+    return 30 if w.args.get("mode", "far") == "near" else FLOPS_PER_UNIT
 
 
 def cpu_sample(w, n_tracks=4, sub=(16, 16)):
@@ -137,7 +159,9 @@ def cpu_sample(w, n_tracks=4, sub=(16, 16)):
     dph = (p1 - p0) / nP
     g = [args["grid"][0], (t0, t0 + dth * (sub[0] - 1)), (p0, p0 + dph * sub[1]),
          (nO, sub[0], sub[1])]
-    return {"grid": g, "dtype": "double"}, [list(t) for t in w.tracks[:n_tracks]]
+    tracks = [[np.asarray(a, np.float64) for a in t[:6]] + list(t[6:])
+              for t in w.tracks[:n_tracks]]
+    return {"grid": g, "dtype": "double", "mode": args.get("mode", "far")}, tracks
 
 
 def time_cpu_oracle(w, nthreads, n_tracks=4, sub=(16, 16), kind=None):
@@ -149,7 +173,7 @@ def time_cpu_oracle(w, nthreads, n_tracks=4, sub=(16, 16), kind=None):
     a, tracks = cpu_sample(w, n_tracks, sub)
     t0 = time.perf_counter()
     host.calculate_spectrum(a, tracks, w.time_step, comp="total", kind=lib_kind,
-                            nthreads=nthreads)
+                            nthreads=nthreads, L_screen=w.L_screen)
     el = time.perf_counter() - t0
     pts = int(np.prod(a["grid"][-1])) * sum(len(t[0]) - 1 for t in tracks)
     return pts / el / 1e9, el, pts, kind
@@ -170,8 +194,8 @@ def reference_arm(args):
             vals.append((v, el))
     v = float(np.median([x[0] for x in vals]))
     ms = float(np.mean([x[1] for x in vals])) * 1e3
-    sample = (f"2 tracks x 4000 steps on the full 512-omega axis x 8 theta x 16 phi "
-              f"(the first nodes of the grid), FP64, {nth} threads")
+    sample = (f"first 2 tracks on the full omega axis x 8 x 16 directions or screen "
+              f"points (the first nodes of the grid), FP64, {nth} threads")
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -208,11 +232,14 @@ def main():
 
     L = _lib.lib()
     w = make_workload(args)
+    mode = w.args.get("mode", "far")
     a = ohost.init_args(dict(w.args, dtype="double"))
     nO, nT, nP = (int(v) for v in a["gridNodeNums"])
     P = nO * nT * nP
-    grid = make_grid("far", ohost.device_axes(a), (nO, nT, nP), torch.float64, device)
-    batch = pack_tracks(w.tracks, np.float64, 1, w.time_step, device=device)
+    grid = make_grid(mode, ohost.device_axes(a), (nO, nT, nP), torch.float64, device,
+                     L_screen=w.L_screen or 0.0)
+    track_np = np.float32 if args.workload == "ragged" else np.float64
+    batch = pack_tracks(w.tracks, track_np, 1, w.time_step, device=device)
     out = torch.zeros((1, nP, nT, nO), dtype=torch.float64, device=device)
     wsp = Workspace(device)
     pt_steps = w.pt_steps
@@ -268,17 +295,20 @@ def main():
     _lib.check(L.sr_probe_fp32_peak(ctypes.byref(tf_s), ctypes.byref(tf_p),
                                     ctypes.c_void_p(stream.cuda_stream)))
     kern_avg_ms = kern_ms.value / max(kern_n.value, 1)
-    achieved = pt_steps * FLOPS_PER_UNIT / (kern_avg_ms * 1e-3) / 1e12
+    fpu = flops_per_unit(w)
+    achieved = pt_steps * fpu / (kern_avg_ms * 1e-3) / 1e12
     peak = max(tf_s.value, tf_p.value)
     clk = clocks.summary()
     roofline = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak if peak else None,
                 "traffic": None,
-                "kernel": "far_mixed_kernel (32 omega points per lane, 8 warps per CTA)",
+                "kernel": ("near_mixed_kernel (8 omega points per lane, 8 warps per CTA)"
+                           if mode == "near" else
+                           "far_mixed_kernel (32 omega points per lane, 8 warps per CTA)"),
                 "kernel_ms_avg": kern_avg_ms,
-                "flops_per_unit": FLOPS_PER_UNIT,
-                "frac_canonical_18_flops": (achieved * CANONICAL_FLOPS / FLOPS_PER_UNIT / peak
-                                            if peak else None),
+                "flops_per_unit": fpu,
+                "frac_canonical_18_flops": (achieved * CANONICAL_FLOPS / fpu / peak
+                                            if peak and mode == "far" else None),
                 "peak_source": ("measured on this GPU by sr_probe_fp32_peak (FFMA / FFMA2 "
                                 f"throughput: {tf_s.value:.1f} / {tf_p.value:.1f} TFLOP/s); "
                                 "MEASURED_PEAKS.json has no FP32 figure"),
@@ -289,7 +319,7 @@ def main():
     # --- accuracy and throughput of the plain FP64 kernel on a track subset ---
     fp64 = None
     if not args.no_fp64:
-        sub_tr = w.tracks[:2]
+        sub_tr = [[np.asarray(v, np.float64) for v in t[:6]] + list(t[6:]) for t in w.tracks[:2]]
         sb = pack_tracks(sub_tr, np.float64, 1, w.time_step, device=device)
         o64 = torch.zeros_like(out)
         omx = torch.zeros_like(out)
@@ -320,15 +350,17 @@ def main():
     e2e = None
     if not args.no_e2e:
         n_e2e = args.e2e_steps or args.steps
-        calc = SynchRad({"grid": w.args["grid"], "dtype": "mixed"})
+        calc = SynchRad({"grid": w.args["grid"], "dtype": "mixed", "mode": mode})
         host_tracks = [list(t) for t in w.tracks]
-        calc.calculate_spectrum(host_tracks, timeStep=w.time_step, verbose=False)  # warm
+        calc.calculate_spectrum(host_tracks, timeStep=w.time_step, verbose=False,
+                                L_screen=w.L_screen)  # warm
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(n_e2e):
-            calc.calculate_spectrum(host_tracks, timeStep=w.time_step, verbose=False)
+            calc.calculate_spectrum(host_tracks, timeStep=w.time_step, verbose=False,
+                                    L_screen=w.L_screen)
         torch.cuda.synchronize()
         el = time.perf_counter() - t0
         if dist:
@@ -349,8 +381,8 @@ def main():
         nth = os.cpu_count() or 1
         v, el, pts, kind = time_cpu_oracle(w, nth)
         cpu = {"value": v, "unit": UNIT, "cores": nth, "kind": kind,
-               "sample": f"first 4 tracks x 4000 steps on the full 512-omega axis x 16 theta "
-                         f"x 16 phi, FP64, {nth} threads, {el:.1f} s"}
+               "sample": f"first 4 tracks on the full omega axis x 16 x 16 directions or "
+                         f"screen points, FP64, {nth} threads, {el:.1f} s"}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
@@ -359,10 +391,13 @@ def main():
                 "dtype": "f32 (mixed: double-float phase, compensated FP32 sums, FP64 spectrum)",
                 "data": "synthetic",
                 "config": {"workload": w.name, "n_tracks": len(w.tracks),
-                           "steps_per_track": args.track_steps, "grid": list(args.grid),
+                           "steps_per_track": (int(w.pt_steps // P // len(w.tracks)) + 1
+                                               if args.workload != "ragged" else "500-20000"),
+                           "grid": list(w.args["grid"][-1]),
                            "comp": "total", "pt_steps_per_step": pt_steps,
                            "l2": "flushed before every timed step (256 MB write, counted); "
-                                 "step records (262 MB) exceed L2",
+                                 f"step records ({batch.total_steps * 64 / 1e6:.0f} MB) "
+                                 "exceed L2",
                            "parallelism": f"replicas x{ws} (tracks independent)"},
                 "e2e": e2e, "gpu_launches": 3 * args.steps * 1,
                 "clocks": clk, "roofline": roofline, "cpu_baseline": cpu, "fp64_port": fp64}

@@ -101,6 +101,7 @@ FarMixedParams far_mixed_params(const sr_tracks *t, const sr_grid *g, int comp,
   p.sin_phi = (const double *)g->sin_phi;
   p.cos_phi = (const double *)g->cos_phi;
   p.form_factor = (const double *)g->form_factor;
+  p.L_screen = g->L_screen;
   p.comp = comp;
   p.n_out = n_outputs(comp);
   for (int i = 0; i < p.n_out; ++i) p.out[i] = (double *)out[i];
@@ -141,7 +142,9 @@ extern "C" int64_t sr_workspace_bytes(const sr_tracks *t, const sr_grid *g, int 
         far_mixed_choose(g->n_omega, g->n_theta * g->n_phi, t->n_tracks, n_sm_of_current_device());
     return (int64_t)far_mixed_workspace(t->total_steps, P, nout, t->n_snaps ? t->n_snaps : 1, cfg);
   }
-  return -1;
+  const FarMixedConfig cfg =
+      near_mixed_choose(g->n_omega, g->n_theta * g->n_phi, t->n_tracks, n_sm_of_current_device());
+  return (int64_t)near_mixed_workspace(t->total_steps, P, nout, t->n_snaps ? t->n_snaps : 1, cfg);
 }
 
 extern "C" int sr_workspace_status(const void *workspace, void *stream) {
@@ -174,7 +177,10 @@ extern "C" int sr_spectrum(const sr_tracks *t, const sr_grid *g, int comp, int p
       return launch_far_mixed(far_mixed_params(t, g, comp, out), cfg, workspace,
                               workspace_bytes, s);
     }
-    return fail(SR_ERR_UNSUPPORTED, "mixed precision near field is not available");
+    const FarMixedConfig cfg = near_mixed_choose(g->n_omega, g->n_theta * g->n_phi,
+                                                 t->n_tracks, n_sm_of_current_device());
+    return launch_near_mixed(far_mixed_params(t, g, comp, out), cfg, workspace,
+                             workspace_bytes, s);
   }
 
   PortParams p;

@@ -106,6 +106,27 @@ __device__ __forceinline__ df df_mul_raw(df a, df b) {
   return df{p, e};
 }
 
+__device__ __forceinline__ df df_neg(df a) { return df{-a.hi, -a.lo}; }
+__device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
+// sqrt of a positive double-float: float root refined by one Newton step on
+// the exact residual a - x^2 (TwoProduct through FMA).
+__device__ __forceinline__ df df_sqrt(df a) {
+  const float x = sqrtf(a.hi);
+  if (x == 0.f) return df{0.f, 0.f};
+  const float p = x * x;
+  const float e = __fmaf_rn(x, x, -p);
+  const float r = ((a.hi - p) - e) + a.lo;
+  return fast_two_sum(x, r * (0.5f / x));
+}
+// a / b for double-floats: quotient, exact remainder, one correction.
+__device__ __forceinline__ df df_div(df a, df b) {
+  const float q1 = a.hi / b.hi;
+  const df qb = df_mul(df{q1, 0.f}, b);
+  const df r = df_sub(a, qb);
+  const float q2 = (r.hi + r.lo) / b.hi;
+  return fast_two_sum(q1, q2);
+}
+
 // 2*pi split for the Cody-Waite style reduction below.
 #define SR_TWO_PI_HI 6.28318548202514648f
 #define SR_TWO_PI_LO (-1.74845553146951720e-07f)

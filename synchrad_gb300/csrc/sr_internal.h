@@ -50,6 +50,7 @@ struct FarMixedParams {
   uint32_t n_omega, n_theta, n_phi;
   const double *omega, *sin_theta, *cos_theta, *sin_phi, *cos_phi,
       *form_factor;
+  double L_screen;     // near field: distance to the screen
   int comp;
   int n_out;
   // decomposition
@@ -83,6 +84,15 @@ size_t far_mixed_workspace(int64_t total_steps, uint64_t n_points, int n_out,
                            uint32_t n_snaps, const FarMixedConfig &cfg);
 int launch_far_mixed(FarMixedParams p, const FarMixedConfig &cfg,
                      void *workspace, size_t ws_bytes, cudaStream_t stream);
+
+// The mixed-precision near field (same parameter block; n_theta holds n_R,
+// sin_theta the radius axis, L_screen the screen distance).
+FarMixedConfig near_mixed_choose(uint32_t n_omega, uint32_t n_screen, uint32_t n_tracks,
+                                 int n_sm);
+size_t near_mixed_workspace(int64_t total_steps, uint64_t n_points, int n_out,
+                            uint32_t n_snaps, const FarMixedConfig &cfg);
+int launch_near_mixed(FarMixedParams p, const FarMixedConfig &cfg, void *workspace,
+                      size_t ws_bytes, cudaStream_t stream);
 
 // sr_api.cu: argument checks and parameter packing shared by entry points.
 int validate_spectrum_args(const sr_tracks *t, const sr_grid *g, int comp,

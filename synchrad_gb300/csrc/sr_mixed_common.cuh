@@ -1,0 +1,90 @@
+// Device helpers shared by the mixed-precision far- and near-field kernels.
+#pragma once
+
+#include "sr_common.cuh"
+#include "sr_internal.h"
+
+namespace sr {
+namespace {
+
+constexpr int kStage = 128;         // steps per TMA stage
+constexpr int kFoldStages = 8;      // FP32 sums fold into compensated pairs every 1024 steps
+constexpr int kRecF4 = 4;           // float4 per step record (64 bytes)
+constexpr float kPiLo = 3.14159265358979f * (1.0f - 4e-6f);
+constexpr float kPiHi = 3.14159265358979f * (1.0f + 4e-6f);
+
+__device__ __forceinline__ uint32_t lower_bound_i64(const int64_t *a, uint32_t n,
+                                                    int64_t v) {
+  uint32_t lo = 0, hi = n;  // first index in [0, n) with a[i] >= v, or n
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (a[mid] < v) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+// Track range [t0, t1) of subset `sub`: tracks whose first step lies in
+// [sub*total/n_sub, (sub+1)*total/n_sub), so subsets carry equal step counts.
+__device__ __forceinline__ void subset_tracks(const FarMixedParams &p, uint32_t sub,
+                                              uint32_t &t0, uint32_t &t1) {
+  const int64_t tot = p.total_steps;
+  t0 = (sub == 0) ? 0u
+                  : lower_bound_i64(p.offsets, p.n_tracks, (tot * (int64_t)sub) / p.n_sub);
+  t1 = (sub + 1 == p.n_sub)
+           ? p.n_tracks
+           : lower_bound_i64(p.offsets, p.n_tracks, (tot * (int64_t)(sub + 1)) / p.n_sub);
+}
+
+__device__ __forceinline__ uint32_t track_body(const FarMixedParams &p, uint32_t t) {
+  const int64_t n = p.offsets[t + 1] - p.offsets[t];
+  const uint32_t it_end = p.it_end[t];
+  if (n < 1 || it_end < 1) return 0;
+  return (uint32_t)min((int64_t)it_end - 1, n - 1);
+}
+
+// exp(i 2 pi w tau) for a double-float frequency in revolutions: the phase is
+// formed in double-float, its whole revolutions are dropped (p - rint(p) is
+// exact), and the fraction goes to the SFU sin/cos.
+__device__ __forceinline__ void phasor_rev(float wh, float wl, float th, float tl, float &s,
+                                           float &c) {
+  const float p = wh * th;
+  float e = __fmaf_rn(wh, th, -p);
+  e = __fmaf_rn(wh, tl, e);
+  e = __fmaf_rn(wl, th, e);
+  const float n = rintf(p);
+  const float f = (p - n) + e;
+  __sincosf(f * 6.28318530717958648f, &s, &c);
+}
+
+// (zr + i zi) * (rc + i rs) for two points at once, factors given as pairs.
+__device__ __forceinline__ void rot2p(float2 zr, float2 zi, float2 rc, float2 rs, float2 nrs,
+                                      float2 &or_, float2 &oi) {
+  const float2 u = __fmul2_rn(zi, nrs);
+  const float2 v = __fmul2_rn(zr, rs);
+  or_ = __ffma2_rn(zr, rc, u);
+  oi = __ffma2_rn(zi, rc, v);
+}
+
+__device__ __forceinline__ void cmul(float ar, float ai, float br, float bi, float &cr,
+                                     float &ci) {
+  cr = ar * br - ai * bi;
+  ci = ar * bi + ai * br;
+}
+
+// out[c][k*P + g] += sum over subsets (fixed order) of partial[sub][c][k][g]
+__global__ void mixed_reduce_kernel(FarMixedParams p) {
+  const uint64_t P = (uint64_t)p.n_omega * p.n_theta * p.n_phi;
+  const uint64_t per = (uint64_t)p.n_snaps * P;
+  const uint64_t total = per * p.n_out;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t c = (uint32_t)(i / per);
+    const uint64_t r = i - (uint64_t)c * per;
+    double acc = 0.0;
+    for (uint32_t s = 0; s < p.n_sub; ++s) acc += p.partial[((uint64_t)s * p.n_out + c) * per + r];
+    p.out[c][r] += acc;
+  }
+}
+
+}  // namespace
+}  // namespace sr

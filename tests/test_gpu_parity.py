@@ -78,6 +78,16 @@ def test_golden_mixed_far(name):
     compare(calc.Data["radiation"], case.expected, TOL["mixed"], name)
 
 
+@pytest.mark.parametrize("name", [n for n in gc.names()
+                                  if n.startswith("near_") and not n.endswith("_float")])
+def test_golden_mixed_near(name):
+    """Mixed precision against the FP64 reference on every near-field case."""
+    _need_gpu()
+    case = gc.load(name)
+    calc = run_case(case, dtype="mixed")
+    compare(calc.Data["radiation"], case.expected, TOL["mixed"], name)
+
+
 def test_mixed_is_deterministic():
     _need_gpu()
     case = gc.load("far_total_ragged_wmean")
