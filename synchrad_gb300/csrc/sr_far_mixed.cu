@@ -210,6 +210,7 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
     // Lane omega constants (revolutions) and uniformity of its chunk.
     const double w0d = nv > 0 ? p.omega[j0] : 0.0;
     const df d_w0 = df_from_double(w0d * inv2pi);
+    const float w0f = (float)w0d, dwf = (float)dw_glob;
     bool uniform = true;
     float wabs_min = 3.0e38f, wabs_max = 0.f;
     for (int m = 0; m < nv; ++m) {
@@ -471,7 +472,10 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
                 }
               }
             };
-            if (uniform && !fire_here && wabs_max * sm.dc[warp][dsub].adt_max < kPiLo) {
+            // warp-uniform choice: the whole warp runs the tight loop or the
+            // general one (lanes of a warp never diverge between the two)
+            if (__all_sync(0xffffffffu, uniform && !fire_here &&
+                           wabs_max * sm.dc[warp][dsub].adt_max < kPiLo)) {
               const float4 *st = setup + (size_t)dsub * 6;
               const size_t stride = (size_t)dpw * 6;
               for (uint32_t i = 0; i < mcnt; ++i, st += stride) step_fast(st);
@@ -485,23 +489,36 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
                 const uint32_t s = s0 + c0 + i;
                 const bool all_in = wabs_max * adt < kPiLo;
                 const bool all_out = wabs_min * adt > kPiHi;
-                if (uniform && all_in) {
-                  step_fast(st);
-                } else if (!all_out && nv > 0) {
+                // one masked path for every lane of the warp (excluded lanes
+                // carry a zero mask); skipped only when the whole warp is out
+                if (!__all_sync(0xffffffffu, all_out || nv == 0)) {
                   const float4 A = st[0], AT = st[1], R2 = st[2], X = st[3], Y = st[4];
-                  uint32_t mask = 0xffffffffu;
-                  if (!all_in) {
+                  uint32_t mask = (all_out || nv == 0) ? 0u : 0xffffffffu;
+                  if (!all_in && !all_out && nv > 0) {
                     const DirConst &d = sm.dc[warp][dsub];
-                    mask = 0;
+                    if (uniform) {
+                      // included points form an index interval; only points
+                      // inside the guard band need the exact FP64 test
+                      mask = omega_range_bits(w0f, dwf, kPiLo / adt, nv);
+                      uint32_t unc = omega_range_bits(w0f, dwf, kPiHi / adt, nv) & ~mask;
+                      while (unc) {
+                        const int m = __ffs(unc) - 1;
+                        unc &= unc - 1u;
+                        if (exact_mask(p, base, s, it_start, p.omega[j0 + m], d.n0, d.n1, d.cT))
+                          mask |= 1u << m;
+                      }
+                    } else {
+                      mask = 0;
 #pragma unroll 1
-                    for (int m = 0; m < nv; ++m) {
-                      const double wm = p.omega[j0 + m];
-                      const float ph = (float)fabs(wm) * adt;
-                      bool inc;
-                      if (ph < kPiLo) inc = true;
-                      else if (ph > kPiHi) inc = false;
-                      else inc = exact_mask(p, base, s, it_start, wm, d.n0, d.n1, d.cT);
-                      mask |= (uint32_t)inc << m;
+                      for (int m = 0; m < nv; ++m) {
+                        const double wm = p.omega[j0 + m];
+                        const float ph = (float)fabs(wm) * adt;
+                        bool inc;
+                        if (ph < kPiLo) inc = true;
+                        else if (ph > kPiHi) inc = false;
+                        else inc = exact_mask(p, base, s, it_start, wm, d.n0, d.n1, d.cT);
+                        mask |= (uint32_t)inc << m;
+                      }
                     }
                   }
                   float zs, zc;
@@ -522,7 +539,7 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
 #pragma unroll
                         for (int e = 0; e < 2; ++e) {
                           const int m = h * (K / 2) + 2 * q + e;
-                          const df wr = df_from_double(p.omega[j0 + min(m, nv - 1)] * inv2pi);
+                          const df wr = df_from_double(p.omega[j0 + min(m, max(nv - 1, 0))] * inv2pi);
                           float ss, cc;
                           phasor_rev(wr.hi, wr.lo, A.x, A.y, ss, cc);
                           float2 &zr = h ? ZrB : ZrA;

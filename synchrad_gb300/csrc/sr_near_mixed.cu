@@ -187,6 +187,7 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
     }
     const double w0d = nv > 0 ? p.omega[j0] : 0.0;
     const df d_w0 = df_from_double(w0d * inv2pi);
+    const float w0f = (float)w0d, dwf = (float)dw_glob;
     bool uniform = true;
     float wabs_min = 3.0e38f, wabs_max = 0.f;
     for (int m = 0; m < nv; ++m) {
@@ -424,7 +425,10 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
             __syncwarp();
             const bool fire_here = snap.fire_it >= (int64_t)(s0 + c0) &&
                                    snap.fire_it < (int64_t)(s0 + c0 + mcnt);
-            if (uniform && !fire_here && wabs_max * sm.sc[warp][dsub].adt_max < kPiLo) {
+            // warp-uniform choice: the whole warp runs the tight loop or the
+            // general one (lanes of a warp never diverge between the two)
+            if (__all_sync(0xffffffffu, uniform && !fire_here &&
+                           wabs_max * sm.sc[warp][dsub].adt_max < kPiLo)) {
               const float4 *st = setup + (size_t)dsub * kNSetupF4;
               const size_t stride = (size_t)dpw * kNSetupF4;
               for (uint32_t i = 0; i < mcnt; ++i, st += stride) step_fast(st);
@@ -436,50 +440,81 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
                 const uint32_t s = s0 + c0 + i;
                 const bool all_in = wabs_max * adt < kPiLo;
                 const bool all_out = wabs_min * adt > kPiHi;
-                if (uniform && all_in) {
-                  step_fast(st);
-                } else if (!all_out && nv > 0) {
-                  const float4 A = st[0], F1 = st[1], F2 = st[2], F3 = st[3];
-                  uint32_t mask = 0xffffffffu;
-                  if (!all_in) {
+                // one masked path for every lane of the warp (excluded lanes
+                // carry a zero mask); skipped only when the whole warp is out
+                if (!__all_sync(0xffffffffu, all_out || nv == 0)) {
+                  const float4 A = st[0], F1 = st[1], F2 = st[2], F3 = st[3], R2 = st[4],
+                               X = st[5], Y = st[6];
+                  uint32_t mask = (all_out || nv == 0) ? 0u : 0xffffffffu;
+                  if (!all_in && !all_out && nv > 0) {
                     const ScreenConst &c = sm.sc[warp][dsub];
-                    mask = 0;
+                    if (uniform) {
+                      // included points form an index interval; only points
+                      // inside the guard band need the exact FP64 test
+                      mask = omega_range_bits(w0f, dwf, kPiLo / adt, nv);
+                      uint32_t unc = omega_range_bits(w0f, dwf, kPiHi / adt, nv) & ~mask;
+                      while (unc) {
+                        const int m = __ffs(unc) - 1;
+                        unc &= unc - 1u;
+                        if (exact_mask_near(p, base, s, it_start, p.omega[j0 + m], c.P0, c.P1))
+                          mask |= 1u << m;
+                      }
+                    } else {
+                      mask = 0;
 #pragma unroll 1
-                    for (int m = 0; m < nv; ++m) {
-                      const double wm = p.omega[j0 + m];
-                      const float phd = (float)fabs(wm) * adt;
-                      bool inc;
-                      if (phd < kPiLo) inc = true;
-                      else if (phd > kPiHi) inc = false;
-                      else inc = exact_mask_near(p, base, s, it_start, wm, c.P0, c.P1);
-                      mask |= (uint32_t)inc << m;
-                    }
-                  }
-                  // phasor of point m: recurrence by R (uniform) or its own reseed
-                  float cc, ss;
-                  phasor_rev(d_w0.hi, d_w0.lo, A.x, A.y, ss, cc);
-#pragma unroll
-                  for (int m = 0; m < K; ++m) {
-                    if (m > 0) {
-                      if (uniform) {
-                        const float nc = cc * A.z - ss * A.w;
-                        ss = cc * A.w + ss * A.z;
-                        cc = nc;
-                      } else {
-                        const df wr = df_from_double(p.omega[j0 + min(m, nv - 1)] * inv2pi);
-                        phasor_rev(wr.hi, wr.lo, A.x, A.y, ss, cc);
+                      for (int m = 0; m < nv; ++m) {
+                        const double wm = p.omega[j0 + m];
+                        const float phd = (float)fabs(wm) * adt;
+                        bool inc;
+                        if (phd < kPiLo) inc = true;
+                        else if (phd > kPiHi) inc = false;
+                        else inc = exact_mask_near(p, base, s, it_start, wm, c.P0, c.P1);
+                        mask |= (uint32_t)inc << m;
                       }
                     }
-                    const float g = ((mask >> m) & 1u) ? 1.f : 0.f;
-                    const float2 zr = (m & 1) ? make_float2(0.f, cc) : make_float2(cc, 0.f);
-                    const float2 zi = (m & 1) ? make_float2(0.f, ss) : make_float2(ss, 0.f);
-                    const float2 aa[3] = {make_float2(F1.x * g, F1.x * g),
-                                          make_float2(F1.z * g, F1.z * g),
-                                          make_float2(F2.x * g, F2.x * g)};
-                    const float2 bb[3] = {make_float2(F2.z * g, F2.z * g),
-                                          make_float2(F3.x * g, F3.x * g),
-                                          make_float2(F3.z * g, F3.z * g)};
-                    near_accumulate(acc, m >> 1, zr, zi, bb, aa);
+                  }
+                  // phasors as two packed chains (uniform axis) or one reseed per
+                  // point (non-uniform axis); amplitudes zeroed where masked out
+                  float zs, zc;
+                  phasor_rev(d_w0.hi, d_w0.lo, A.x, A.y, zs, zc);
+                  float2 ZrA = make_float2(zc, zc * A.z - zs * A.w);
+                  float2 ZiA = make_float2(zs, zc * A.w + zs * A.z);
+                  float2 ZrB, ZiB;
+                  rot2p(ZrA, ZiA, make_float2(X.z, X.w), make_float2(Y.x, Y.y),
+                        make_float2(Y.z, Y.w), ZrB, ZiB);
+#pragma unroll
+                  for (int q = 0; q < HP; ++q) {
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                      float2 &zr = h ? ZrB : ZrA;
+                      float2 &zi = h ? ZiB : ZiA;
+                      const int m0 = h * (K / 2) + 2 * q;
+                      if (!uniform) {
+#pragma unroll
+                        for (int e = 0; e < 2; ++e) {
+                          const df wr =
+                              df_from_double(p.omega[j0 + min(m0 + e, max(nv - 1, 0))] * inv2pi);
+                          float ss, cc;
+                          phasor_rev(wr.hi, wr.lo, A.x, A.y, ss, cc);
+                          if (e == 0) { zr.x = cc; zi.x = ss; } else { zr.y = cc; zi.y = ss; }
+                        }
+                      }
+                      const float g0 = ((mask >> m0) & 1u) ? 1.f : 0.f;
+                      const float g1 = ((mask >> (m0 + 1)) & 1u) ? 1.f : 0.f;
+                      const float2 aa[3] = {make_float2(F1.x * g0, F1.y * g1),
+                                            make_float2(F1.z * g0, F1.w * g1),
+                                            make_float2(F2.x * g0, F2.y * g1)};
+                      const float2 bb[3] = {make_float2(F2.z * g0, F2.w * g1),
+                                            make_float2(F3.x * g0, F3.y * g1),
+                                            make_float2(F3.z * g0, F3.w * g1)};
+                      near_accumulate(acc, h * HP + q, zr, zi, bb, aa);
+                    }
+                    if (q + 1 < HP && uniform) {
+                      rot2p(ZrA, ZiA, make_float2(R2.x, R2.y), make_float2(R2.z, R2.w),
+                            make_float2(X.x, X.y), ZrA, ZiA);
+                      rot2p(ZrB, ZiB, make_float2(R2.x, R2.y), make_float2(R2.z, R2.w),
+                            make_float2(X.x, X.y), ZrB, ZiB);
+                    }
                   }
                 }
                 if ((int64_t)s == snap.fire_it) {
