@@ -145,6 +145,33 @@ const char *sr_last_error(void);
 int sr_version(void);
 
 /* ---------------------------------------------------------------------------
+ * Adjoint of the mixed-precision far field, comp 'total', one snapshot.
+ * No counterpart in the reference (it has no gradients).  The |dphase| < pi
+ * mask is held fixed; the omega axis must be uniform.
+ * ------------------------------------------------------------------------- */
+
+/* sr_spectrum (SR_PREC_MIXED, far, SR_COMP_TOTAL, n_snaps = 1) that also
+ * records each track's A_theta, A_phi per point in saved_A
+ * ([n_tracks][P][4] float, written) for sr_far_total_backward.  Same
+ * workspace as sr_spectrum. */
+int sr_far_total_forward_saved(const sr_tracks *tracks, const sr_grid *grid,
+                               double *spectrum, float *saved_A, void *workspace,
+                               size_t workspace_bytes, void *stream);
+
+/* Scratch bytes of sr_far_total_backward for these sizes. */
+int64_t sr_far_total_backward_workspace_bytes(const sr_tracks *tracks,
+                                              const sr_grid *grid);
+
+/* Given dL/dS (grad_spectrum, [P] doubles in the device layout) and the
+ * forward's saved_A, writes dL/dx, dL/dy, dL/dz, dL/dux, dL/duy, dL/duz
+ * (grad_track[0..5], [total_steps] doubles each) and dL/dw (grad_weight,
+ * [n_tracks]).  Phases are recomputed, not stored. */
+int sr_far_total_backward(const sr_tracks *tracks, const sr_grid *grid,
+                          const double *grad_spectrum, const float *saved_A,
+                          double *const *grad_track, double *grad_weight,
+                          void *workspace, size_t workspace_bytes, void *stream);
+
+/* ---------------------------------------------------------------------------
  * Diagnostics.  These have no counterpart in the reference; the benchmark uses
  * them for its roofline figures.
  * ------------------------------------------------------------------------- */

@@ -25,6 +25,7 @@ SOURCES = {
     "sr_port.cu": ["--fmad=false"],
     "sr_far_mixed.cu": [],
     "sr_near_mixed.cu": [],
+    "sr_far_adjoint.cu": [],
     "sr_diag.cu": [],
     "sr_noalloc.cu": [],
 }

@@ -90,7 +90,8 @@ EXPORTS = (
     "sr_far_cartesian_comps_complex", "sr_far_spheric_comps",
     "sr_far_spheric_comps_complex", "sr_near_total", "sr_near_cartesian_comps",
     "sr_near_cartesian_comps_complex", "sr_timing_enable", "sr_timing_read",
-    "sr_probe_fp32_peak", "sr_spectrum_noalloc",
+    "sr_probe_fp32_peak", "sr_spectrum_noalloc", "sr_far_total_forward_saved",
+    "sr_far_total_backward_workspace_bytes", "sr_far_total_backward",
 )
 
 _lock = threading.Lock()
@@ -105,6 +106,15 @@ def _declare(L: ctypes.CDLL) -> None:
     L.sr_spectrum_noalloc.restype = i32
     L.sr_spectrum_noalloc.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid), i32,
                                       ctypes.POINTER(vp), vp]
+    L.sr_far_total_forward_saved.restype = i32
+    L.sr_far_total_forward_saved.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid),
+                                             vp, vp, vp, ctypes.c_size_t, vp]
+    L.sr_far_total_backward_workspace_bytes.restype = ctypes.c_int64
+    L.sr_far_total_backward_workspace_bytes.argtypes = [ctypes.POINTER(SrTracks),
+                                                        ctypes.POINTER(SrGrid)]
+    L.sr_far_total_backward.restype = i32
+    L.sr_far_total_backward.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid), vp, vp,
+                                        ctypes.POINTER(vp), vp, vp, ctypes.c_size_t, vp]
     L.sr_workspace_bytes.restype = ctypes.c_int64
     L.sr_workspace_bytes.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid), i32, i32]
     L.sr_workspace_status.restype = i32

@@ -1,0 +1,123 @@
+"""Differentiable far-field spectrum: ``torch.autograd.Function`` over the
+hand-written adjoint kernel.
+
+``far_total_spectrum(x, y, z, ux, uy, uz, w, layout)`` returns the
+mixed-precision far-field spectrum ``S`` (comp 'total', one snapshot, device
+layout ``[nPhi, nTheta, nOmega]``) of a batch of tracks given as concatenated
+float64 CUDA tensors (CSR order of ``layout.offsets``); its backward calls
+``sr_far_total_backward`` and returns dL/dx .. dL/duz (per step) and dL/dw
+(per track).  The |dphase| < pi mask of the reference is held fixed (it is a
+step function of the coordinates).
+
+The reference has no gradients; this is an extension of its far-field
+integral (``synchrad/kernel_farfield.cl:59-107``).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+from .batch import GridDevice, TrackBatch, Workspace, make_grid, snap_iterations
+
+
+@dataclass
+class FarLayout:
+    """Everything of a batch that is not differentiated."""
+    offsets: torch.Tensor        # int64 [n+1] on the device
+    it_start: torch.Tensor       # int32 [n]
+    it_end: torch.Tensor         # int32 [n]
+    snap_its: torch.Tensor       # int32 [n] (one snapshot per track)
+    dt: float
+    grid: GridDevice
+    workspace: Workspace
+
+    @property
+    def n_tracks(self) -> int:
+        return int(self.offsets.numel() - 1)
+
+    @property
+    def n_points(self) -> int:
+        return int(np.prod(self.grid.n))
+
+
+def make_layout(lengths, dt, host_axes, n, device="cuda") -> FarLayout:
+    """Layout for tracks of the given lengths with the reference's per-track
+    rules (it_start = 0, itEnd = length, one snapshot at the last step)."""
+    device = torch.device(device)
+    lengths = np.asarray(lengths, dtype=np.int64)
+    if np.any(lengths < 1):
+        raise ValueError("every track needs at least one step")
+    offsets = np.zeros(lengths.size + 1, dtype=np.int64)
+    np.cumsum(lengths, out=offsets[1:])
+    snaps = np.concatenate([snap_iterations((0, int(L)), 1) for L in lengths])
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)
+    grid = make_grid("far", host_axes, n, torch.float64, device)
+    return FarLayout(t(offsets), t(np.zeros(lengths.size, np.int32)),
+                     t(lengths.astype(np.uint32).view(np.int32)),
+                     t(snaps.astype(np.uint32).view(np.int32)), float(dt), grid,
+                     Workspace(device))
+
+
+def _tracks_struct(coords, w, layout: FarLayout) -> TrackBatch:
+    return TrackBatch(layout.n_tracks, torch.float64, int(coords[0].numel()), layout.offsets,
+                      list(coords), w, layout.it_start, layout.it_end, layout.snap_its, 1, 1,
+                      layout.dt)
+
+
+class FarTotalSpectrum(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, y, z, ux, uy, uz, w, layout: FarLayout):
+        L = _lib.lib()
+        coords = [c.detach().contiguous() for c in (x, y, z, ux, uy, uz)]
+        for c in coords:
+            if c.dtype != torch.float64 or not c.is_cuda:
+                raise TypeError("track tensors must be float64 CUDA tensors")
+        wd = w.detach().contiguous().to(torch.float64)
+        batch = _tracks_struct(coords, wd, layout)
+        ts, gs = batch.c_struct(), layout.grid.c_struct()
+        nO, nT, nP = layout.grid.n
+        P = layout.n_points
+        spec = torch.zeros((nP, nT, nO), dtype=torch.float64, device=x.device)
+        saved = torch.empty(layout.n_tracks * P * 4, dtype=torch.float32, device=x.device)
+        need = L.sr_workspace_bytes(ctypes.byref(ts), ctypes.byref(gs), 0, _lib.SR_PREC_MIXED)
+        if need < 0:
+            _lib.check(_lib.SR_ERR_INVALID if need == -1 else int(need))
+        ws = layout.workspace.get(max(int(need), 256))
+        stream = ctypes.c_void_p(torch.cuda.current_stream(x.device).cuda_stream)
+        _lib.check(L.sr_far_total_forward_saved(ctypes.byref(ts), ctypes.byref(gs),
+                                                spec.data_ptr(), saved.data_ptr(),
+                                                ws.data_ptr(), ctypes.c_size_t(int(need)),
+                                                stream))
+        ctx.save_for_backward(*coords, wd, saved)
+        ctx.layout = layout
+        return spec
+
+    @staticmethod
+    def backward(ctx, grad_spec):
+        L = _lib.lib()
+        *coords, wd, saved = ctx.saved_tensors
+        layout = ctx.layout
+        batch = _tracks_struct(coords, wd, layout)
+        ts, gs = batch.c_struct(), layout.grid.c_struct()
+        g = grad_spec.detach().contiguous().to(torch.float64)
+        grads = [torch.empty_like(c) for c in coords]
+        gw = torch.empty(layout.n_tracks, dtype=torch.float64, device=g.device)
+        need = L.sr_far_total_backward_workspace_bytes(ctypes.byref(ts), ctypes.byref(gs))
+        if need < 0:
+            _lib.check(_lib.SR_ERR_INVALID)
+        ws = layout.workspace.get(max(int(need), 256))
+        ptrs = (ctypes.c_void_p * 6)(*[t.data_ptr() for t in grads])
+        stream = ctypes.c_void_p(torch.cuda.current_stream(g.device).cuda_stream)
+        _lib.check(L.sr_far_total_backward(ctypes.byref(ts), ctypes.byref(gs), g.data_ptr(),
+                                           saved.data_ptr(), ptrs, gw.data_ptr(), ws.data_ptr(),
+                                           ctypes.c_size_t(int(need)), stream))
+        return (*grads, gw, None)
+
+
+def far_total_spectrum(x, y, z, ux, uy, uz, w, layout: FarLayout) -> torch.Tensor:
+    """Differentiable mixed-precision far-field spectrum (see module docstring)."""
+    return FarTotalSpectrum.apply(x, y, z, ux, uy, uz, w, layout)

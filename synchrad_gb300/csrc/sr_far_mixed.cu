@@ -103,25 +103,6 @@ __global__ void far_prepass_kernel(FarMixedParams p) {
   }
 }
 
-// The reference's mask test evaluated exactly as the FP64 kernel does it
-// (synchrad/kernel_farfield.cl:65-72), for one point and step.
-__device__ __noinline__ bool exact_mask(const FarMixedParams &p, int64_t base, uint32_t s,
-                                        uint32_t it_start, double omega, double n0,
-                                        double n1, double n2) {
-  auto ld = [&](const void *a, int64_t i) -> double {
-    return p.track_f32 ? (double)((const float *)a)[i] : ((const double *)a)[i];
-  };
-  auto phase_at = [&](uint32_t it) -> double {
-    const double time = __dmul_rn((double)(uint32_t)(it_start + it), p.dt);
-    const int64_t g = base + it;
-    const double d = __dadd_rn(__dadd_rn(__dmul_rn(ld(p.x, g), n0), __dmul_rn(ld(p.y, g), n1)),
-                               __dmul_rn(ld(p.z, g), n2));
-    return __dmul_rn(omega, __dsub_rn(time, d));
-  };
-  const double ph = phase_at(s);
-  const double prev = (s == 0) ? 0.0 : phase_at(s - 1);
-  return fabs(__dsub_rn(ph, prev)) < M_PI;
-}
 
 // Per-direction constants, written once per work item.
 struct DirConst {
@@ -296,6 +277,10 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
           const double Br = (double)o[2 * 32] + (double)o[6 * 32];
           const double Bi = (double)o[3 * 32] + (double)o[7 * 32];
           const uint64_t gti = (uint64_t)(j0 + m) + (uint64_t)nO * dir;
+          if (p.save_A != nullptr && ksnap == 0) {  // the adjoint's forward record
+            float4 *sa = reinterpret_cast<float4 *>(p.save_A) + (uint64_t)t * P + gti;
+            *sa = make_float4((float)Ar, (float)Ai, (float)Br, (float)Bi);
+          }
           auto add = [&](int c, double v) {
             part[((uint64_t)c * p.n_snaps + ksnap) * P + gti] += v;
           };
@@ -633,6 +618,14 @@ int dispatch_k(int K, const FarMixedParams &p, int grid, cudaStream_t s) {
 }
 
 }  // namespace
+
+// The far-field step records for another kernel of the library (the adjoint).
+void launch_far_prepass(const FarMixedParams &p, int blocks, cudaStream_t stream) {
+  if (p.track_f32)
+    far_prepass_kernel<float><<<blocks, 256, 0, stream>>>(p);
+  else
+    far_prepass_kernel<double><<<blocks, 256, 0, stream>>>(p);
+}
 
 // Work shape: K points per lane and L lanes per direction (32/L directions per
 // warp).  The widest lane chunk (K = 32) amortises the per-step reseed best;

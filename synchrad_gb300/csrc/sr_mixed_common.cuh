@@ -56,6 +56,26 @@ __device__ __forceinline__ void phasor_rev(float wh, float wl, float th, float t
   __sincosf(f * 6.28318530717958648f, &s, &c);
 }
 
+// The reference's mask test evaluated exactly as the FP64 kernel does it
+// (synchrad/kernel_farfield.cl:65-72), for one point and step.
+__device__ __noinline__ bool exact_mask(const FarMixedParams &p, int64_t base, uint32_t s,
+                                        uint32_t it_start, double omega, double n0,
+                                        double n1, double n2) {
+  auto ld = [&](const void *a, int64_t i) -> double {
+    return p.track_f32 ? (double)((const float *)a)[i] : ((const double *)a)[i];
+  };
+  auto phase_at = [&](uint32_t it) -> double {
+    const double time = __dmul_rn((double)(uint32_t)(it_start + it), p.dt);
+    const int64_t g = base + it;
+    const double d = __dadd_rn(__dadd_rn(__dmul_rn(ld(p.x, g), n0), __dmul_rn(ld(p.y, g), n1)),
+                               __dmul_rn(ld(p.z, g), n2));
+    return __dmul_rn(omega, __dsub_rn(time, d));
+  };
+  const double ph = phase_at(s);
+  const double prev = (s == 0) ? 0.0 : phase_at(s - 1);
+  return fabs(__dsub_rn(ph, prev)) < M_PI;
+}
+
 // Bits j in [0, nv) of a uniform omega chunk (omega_j = w0 + j dw) with
 // |omega_j| < wb: an index interval, found from its two float bounds.
 __device__ __forceinline__ uint32_t omega_range_bits(float w0, float dw, float wb, int nv) {
