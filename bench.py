@@ -40,7 +40,8 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "Gpt·steps/s (spectral pts × track steps), mixed vs FP64 at ≤1e-5 rel err"
 UNIT = "Gpt·steps/s"
-FLOPS_PER_UNIT = 14      # far field, mixed: 2 FMUL + 6 FFMA per point-step (see DESIGN.md)
+FLOPS_PER_UNIT = 14      # far field, mixed: 2 FMUL + 6 FFMA per point-step
+ADJ_FLOPS_PER_UNIT = 22  # far adjoint: 8 FFMA (E and F sums) + 1 FMUL + 2 FFMA (rotation)
 CANONICAL_FLOPS = 18     # the 3-component formulation's count
 
 
@@ -50,10 +51,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="far", choices=["far", "near", "ragged"],
+    ap.add_argument("--workload", default="far", choices=["far", "near", "ragged", "adjoint"],
                     help="far: the headline configuration (default); near: 2048 helical "
                          "tracks on a screen at 20 undulator lengths; ragged: 8192 FP32 "
-                         "betatron tracks of 500-20000 steps")
+                         "betatron tracks of 500-20000 steps; adjoint: forward and "
+                         "backward of sum(g * S) for 256 tracks x 2000 steps on 128 x 32 x 32")
     ap.add_argument("--tracks", type=int, default=None)
     ap.add_argument("--track-steps", type=int, default=None)
     ap.add_argument("--grid", type=int, nargs=3, default=None)
@@ -139,6 +141,10 @@ def make_workload(args):
         if args.track_steps is not None:
             kw["n_steps"] = args.track_steps
         return wl.c5_near_helical(**kw)
+    if args.workload == "adjoint":
+        if args.track_steps is not None:
+            kw["n_steps"] = args.track_steps
+        return wl.c4_adjoint(**kw)
     if args.track_steps is not None:
         kw["steps_range"] = (max(2, args.track_steps // 40), args.track_steps)
     return wl.c3_betatron_ragged(**kw)
@@ -208,10 +214,131 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def adjoint_main(args):
+    """Forward (mixed far field, amplitudes kept) and backward (adjoint kernel)
+    of L = sum(g * S) on the adjoint workload; one step = forward + backward,
+    L2 flushed before each.  Reports both times and their ratio."""
+    import torch
+    from oracle import host as ohost
+    from synchrad_gb300 import _lib
+    from synchrad_gb300.autograd import far_total_spectrum, make_layout
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        dist = None
+    device = torch.device("cuda", local if ws > 1 else 0)
+    torch.cuda.set_device(device)
+    L = _lib.lib()
+    w = make_workload(args)
+    a = ohost.init_args(dict(w.args, dtype="double"))
+    nO, nT, nP = (int(v) for v in a["gridNodeNums"])
+    lengths = [len(t[0]) for t in w.tracks]
+    layout = make_layout(lengths, w.time_step, ohost.device_axes(a), (nO, nT, nP), device)
+    coords = [torch.tensor(np.concatenate([np.asarray(t[c], np.float64) for t in w.tracks]),
+                           device=device, requires_grad=True) for c in range(6)]
+    wt = torch.tensor([float(t[6]) for t in w.tracks], dtype=torch.float64, device=device,
+                      requires_grad=True)
+    gen = torch.Generator(device="cpu").manual_seed(0)
+    gmat = torch.rand((nP, nT, nO), generator=gen, dtype=torch.float64).to(device)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+    stream = torch.cuda.current_stream(device)
+    pt_steps = w.pt_steps
+
+    def one_step(ev=None):
+        flush.fill_(1.0)
+        for c in coords + [wt]:
+            c.grad = None
+        if ev:
+            ev[0].record(stream)
+        S = far_total_spectrum(*coords, wt, layout)
+        if ev:
+            ev[1].record(stream)
+            _lib.check(L.sr_timing_enable(1))
+        S.backward(gmat)
+        if ev:
+            _lib.check(L.sr_timing_enable(0))
+            ev[2].record(stream)
+
+    for _ in range(args.warmup):
+        one_step()
+    torch.cuda.synchronize()
+    _lib.check(L.sr_timing_read(None, None))
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    try:
+        gpu_id = "GPU-" + str(torch.cuda.get_device_properties(device).uuid)
+    except Exception:
+        gpu_id = str(device.index)
+    with ClockSampler(gpu_id) as clocks:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e_start = torch.cuda.Event(enable_timing=True)
+        e_end = torch.cuda.Event(enable_timing=True)
+        e_start.record(stream)
+        for k in range(args.steps):
+            one_step(evs[k])
+        e_end.record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    kern_ms = ctypes.c_double(0)
+    kern_n = ctypes.c_int(0)
+    _lib.check(L.sr_timing_read(ctypes.byref(kern_ms), ctypes.byref(kern_n)))
+    elapsed = e_start.elapsed_time(e_end)
+    if dist:
+        t = torch.tensor([elapsed], device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    fwd_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in evs]))
+    bwd_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in evs]))
+    ms_per_step = elapsed / args.steps
+    tf_s = ctypes.c_double(0)
+    tf_p = ctypes.c_double(0)
+    _lib.check(L.sr_probe_fp32_peak(ctypes.byref(tf_s), ctypes.byref(tf_p),
+                                    ctypes.c_void_p(stream.cuda_stream)))
+    peak = max(tf_s.value, tf_p.value)
+    kern_avg = kern_ms.value / max(kern_n.value, 1)
+    achieved = pt_steps * ADJ_FLOPS_PER_UNIT / (kern_avg * 1e-3) / 1e12
+    if rank == 0:
+        line = {"metric": "Gpt·steps/s through forward + backward of sum(g·S) (far field)",
+                "value": pt_steps * ws * args.steps / (elapsed * 1e-3) / 1e9, "unit": UNIT,
+                "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None,
+                "dtype": "f32 (mixed: double-float phase, FP32 sums, FP64 gradients)",
+                "data": "synthetic",
+                "config": {"workload": w.name, "n_tracks": len(w.tracks),
+                           "steps_per_track": int(lengths[0]), "grid": [nO, nT, nP],
+                           "pt_steps_per_step": pt_steps,
+                           "l2": "flushed before every timed step (256 MB write, counted)",
+                           "parallelism": f"replicas x{ws} (tracks independent)"},
+                "adjoint": {"forward_ms": fwd_ms, "backward_ms": bwd_ms,
+                            "backward_over_forward": bwd_ms / fwd_ms,
+                            "adj_far_kernel_ms": kern_avg},
+                "e2e": None, "gpu_launches": 8 * args.steps,
+                "clocks": clocks.summary(),
+                "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak,
+                             "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+                             "traffic": None, "kernel": "adj_far_kernel",
+                             "flops_per_unit": ADJ_FLOPS_PER_UNIT,
+                             "peak_source": "measured on this GPU by sr_probe_fp32_peak"},
+                "cpu_baseline": None}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
+        return
+    if args.workload == "adjoint":
+        adjoint_main(args)
         return
     import torch
     ws, rank, local = dist_env()

@@ -236,3 +236,69 @@ def test_adjoint_rejects_unsupported():
     rc = L.sr_far_total_forward_saved(ctypes.byref(ts1), ctypes.byref(gs), S.data_ptr(),
                                       None, None, ctypes.c_size_t(0), None)
     assert rc == _lib.SR_ERR_INVALID
+
+
+def make_edge_case(seed=9):
+    """Tracks of 1, 2, 257 and 300 steps (an empty track, a single step, a
+    one-step second work item); 37 omega points (not a multiple of the
+    8-point blocks); a coarse time step so that |dphase| < pi excludes the
+    upper part of the omega axis on part of each track."""
+    rng = np.random.default_rng(seed)
+    dt = 1.0 / 8
+    tracks = []
+    for L, g in ((1, 10.0), (2, 10.2), (257, 9.8), (300, 10.1)):
+        tr = wl.undulator_track(g, 0.5, 40, dt, x0=rng.normal(0, 0.05),
+                                weight=float(rng.uniform(0.5, 2.0)))
+        tracks.append([np.ascontiguousarray(a[:L]) for a in tr[:6]] + tr[6:])
+    f1 = wl.fundamental(10.0, 0.5)
+    om = 2 * np.pi * f1 * np.linspace(0.5, 5.0, 37)
+    theta = np.linspace(0.0, 1.0 / 10.0, 3)
+    phi = np.linspace(0.0, np.pi, 2, endpoint=False)
+    axes = [np.ascontiguousarray(a, dtype=np.float64)
+            for a in (om, np.sin(theta), np.cos(theta), np.sin(phi), np.cos(phi))]
+    n = (om.size, theta.size, phi.size)
+    gmat = rng.uniform(0.5, 1.5, size=(n[2], n[1], n[0]))
+    return tracks, dt, axes, n, gmat
+
+
+def test_edge_case_has_a_partial_mask():
+    """The coarse case really exercises the per-point mask."""
+    tracks, dt, axes, n, _ = make_edge_case()
+    tr = tracks[3]
+    nvec = np.array([axes[1][2] * axes[4][1], axes[1][2] * axes[3][1], axes[2][2]])
+    time = np.arange(tr[0].size) * dt
+    ph = axes[0][None, :] * (time - (tr[0] * nvec[0] + tr[1] * nvec[1] + tr[2] * nvec[2]))[:, None]
+    d = np.abs(np.diff(ph, axis=0)) < np.pi
+    assert 0.05 < d.mean() < 0.95
+
+
+@pytest.mark.gpu
+def test_adjoint_edge_cases():
+    _need_gpu()
+    tracks, dt, axes, n, gmat = make_edge_case()
+    g_ref, gw_ref, S_ref = torch_gradient(tracks, dt, axes, gmat)
+    g_gpu, gw_gpu, S_gpu = cuda_gradient(tracks, dt, axes, n, gmat)
+    assert rel_l2(S_gpu, S_ref) <= TOL_FWD
+    _, offsets, _, _ = concat(tracks)
+    # the one-step track contributes nothing
+    for c in range(6):
+        assert np.all(g_gpu[c][offsets[0]:offsets[1]] == 0.0)
+    assert gw_gpu[0] == 0.0
+    pos = rel_l2(np.concatenate(g_gpu[:3]), np.concatenate(g_ref[:3]))
+    mom = rel_l2(np.concatenate(g_gpu[3:]), np.concatenate(g_ref[3:]))
+    wts = rel_l2(gw_gpu[1:], gw_ref[1:])
+    print(f"edge cases vs autograd: positions {pos:.2e}, momenta {mom:.2e}, weights {wts:.2e}")
+    assert pos <= TOL_ADJ_AUTOGRAD
+    assert mom <= TOL_ADJ_AUTOGRAD
+    assert wts <= TOL_ADJ_AUTOGRAD
+
+
+@pytest.mark.gpu
+def test_adjoint_deterministic():
+    _need_gpu()
+    tracks, dt, axes, n, gmat = make_case(True, seed=4)
+    g1, w1, _ = cuda_gradient(tracks, dt, axes, n, gmat)
+    g2, w2, _ = cuda_gradient(tracks, dt, axes, n, gmat)
+    for c in range(6):
+        assert np.array_equal(g1[c], g2[c])
+    assert np.array_equal(w1, w2)
