@@ -187,6 +187,23 @@ def c4_adjoint(n_tracks=256, n_steps=2000, grid=(128, 32, 32), seed=0,
                     notes={"seed": seed})
 
 
+def perturbed_tracks(tracks, rel=1e-3, seed=1):
+    """Copies of ``tracks`` with x, y scaled by (1 + rel N(0,1)) and the
+    momenta by (1 + rel N(0,1)) (gamma changes by about the same relative
+    amount), one draw per track: the target tracks of the adjoint workload."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for t in tracks:
+        fx, fu = 1.0 + rel * rng.standard_normal(2)
+        c = [np.asarray(a).copy() for a in t[:6]]
+        c[0] *= fx
+        c[1] *= fx
+        for k in (3, 4, 5):
+            c[k] *= fu
+        out.append(c + list(t[6:]))
+    return out
+
+
 def c5_near_helical(n_tracks=2048, n_steps=8000, grid=(256, 64, 64), seed=0,
                     n_periods=50) -> Workload:
     """2048 electrons in a helical undulator, gamma ~ N(300, 2%), 8000 steps,

@@ -302,3 +302,64 @@ def test_adjoint_deterministic():
     for c in range(6):
         assert np.array_equal(g1[c], g2[c])
     assert np.array_equal(w1, w2)
+
+
+TOL_MISFIT_E2E = 1e-3  # end to end: dL/dS from the mixed spectrum (see the test)
+
+
+@pytest.mark.gpu
+def test_misfit_loss_matches_finite_differences():
+    """The adjoint workload's loss: weighted L2 misfit L = sum(((S - T)/max T)^2)
+    against the spectrum T of the same tracks with x, y and momenta perturbed
+    1e-3 relative, checked against fourth-order finite differences of the FP64
+    oracle on 32 coordinates.
+
+    * adjoint kernel: dL/dS = 2 (S - T)/max(T)^2 formed from the FP64 spectrum
+      and passed to the backward: TOL_ADJ_FD;
+    * end to end (mixed forward, autograd of the loss, adjoint): S - T is about
+      1e-3 of S, so the ~1e-6 relative error of the mixed spectrum enters
+      dL/dS amplified a thousandfold: TOL_MISFIT_E2E.
+    """
+    _need_gpu()
+    from synchrad_gb300.autograd import far_total_spectrum, make_layout
+    tracks, dt, axes, n, _ = make_case(True, seed=6)
+    target = sum(oracle_track_spectrum(t[:6], t[6], dt, axes, n)
+                 for t in wl.perturbed_tracks(tracks, 1e-3, seed=1))
+    inv = 1.0 / target.max()
+    lengths, offsets, coords, weights = concat(tracks)
+    layout = make_layout(lengths, dt, axes, n)
+    per_track = [oracle_track_spectrum(t[:6], t[6], dt, axes, n) for t in tracks]
+    total = sum(per_track)
+
+    def gradients(grad_from_fp64):
+        ts = [torch.tensor(c, dtype=torch.float64, device="cuda", requires_grad=True)
+              for c in coords]
+        w = torch.tensor(weights, dtype=torch.float64, device="cuda", requires_grad=True)
+        S = far_total_spectrum(*ts, w, layout)
+        if grad_from_fp64:
+            S.backward(torch.tensor(2.0 * (total - target) * inv * inv, device="cuda"))
+        else:
+            (((S - torch.tensor(target, device="cuda")) * inv) ** 2).sum().backward()
+        return [t.grad.cpu().numpy() for t in ts]
+
+    g64, gmx = gradients(True), gradients(False)
+    got64, gotmx, exp = [], [], []
+    for (t, c, s) in pick_coordinates(tracks, 32, seed=23):
+        base = tracks[t]
+        v = base[c][s]
+        h = 1e-5 * (max(1.0, abs(v)) if c >= 3 else 1.0)
+        others = total - per_track[t]
+
+        def L_of(delta):
+            tr = [a.copy() for a in base[:6]]
+            tr[c][s] = v + delta
+            St = oracle_track_spectrum(tr, base[6], dt, axes, n)
+            return float(np.sum(((others + St - target) * inv) ** 2))
+
+        exp.append((8.0 * (L_of(h) - L_of(-h)) - (L_of(2 * h) - L_of(-2 * h))) / (12.0 * h))
+        got64.append(g64[c][offsets[t] + s])
+        gotmx.append(gmx[c][offsets[t] + s])
+    e64, emx = rel_l2(got64, exp), rel_l2(gotmx, exp)
+    print(f"misfit loss vs finite differences: adjoint {e64:.2e}, end to end {emx:.2e}")
+    assert e64 <= TOL_ADJ_FD
+    assert emx <= TOL_MISFIT_E2E
