@@ -63,6 +63,11 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="skip the work-shape autotuner (default shape)")
+    ap.add_argument("--tune-budget-ms", type=float, default=6000.0)
+    ap.add_argument("--no-graph", action="store_true",
+                    help="direct sr_spectrum calls instead of CUDA-graph replay")
     return ap.parse_args()
 
 
@@ -366,7 +371,8 @@ def main():
 
     from oracle import host as ohost
     from synchrad_gb300 import _lib
-    from synchrad_gb300.batch import Workspace, make_grid, pack_tracks, run_spectrum
+    from synchrad_gb300.batch import (SpectrumGraph, Workspace, autotune, current_config,
+                                      make_grid, pack_tracks, run_spectrum)
     from synchrad_gb300.calc import SynchRad
 
     L = _lib.lib()
@@ -385,17 +391,31 @@ def main():
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
     stream = torch.cuda.current_stream(device)
 
-    def one_step():
+    tune = None
+    if not args.no_tune:
+        t0 = time.perf_counter()
+        tune = autotune(batch, grid, "total", _lib.SR_PREC_MIXED, args.tune_budget_ms, stream)
+        tune["wall_s"] = time.perf_counter() - t0
+    shape = current_config(batch, grid, "total", _lib.SR_PREC_MIXED)
+    graph = None
+    if not args.no_graph:
+        graph = SpectrumGraph(batch, grid, "total", _lib.SR_PREC_MIXED, [out], wsp)
+
+    def one_step(direct=False):
         flush.fill_(1.0)
         out.zero_()
-        run_spectrum(batch, grid, "total", _lib.SR_PREC_MIXED, [out], workspace=wsp,
-                     stream=stream)
+        if graph is not None and not direct:
+            graph.launch(stream)
+        else:
+            run_spectrum(batch, grid, "total", _lib.SR_PREC_MIXED, [out], workspace=wsp,
+                         stream=stream)
 
     for _ in range(args.warmup):
         one_step()
     torch.cuda.synchronize()
     _lib.check(L.sr_timing_read(None, None))  # clear
-    _lib.check(L.sr_timing_enable(1))
+    if graph is None:
+        _lib.check(L.sr_timing_enable(1))
     try:
         gpu_id = "GPU-" + str(torch.cuda.get_device_properties(device).uuid)
     except Exception:
@@ -413,13 +433,21 @@ def main():
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
+    _lib.check(L.sr_workspace_status(ctypes.c_void_p(wsp.buf.data_ptr()),
+                                     ctypes.c_void_p(stream.cuda_stream)))
+    elapsed_ms = ev0.elapsed_time(ev1)
+    graph_spec = out.clone()
+    if graph is not None:
+        # the graph's kernels are not timed one by one: time the dominant kernel
+        # on one direct call of the same shape
+        _lib.check(L.sr_timing_enable(1))
+        one_step(direct=True)
+        torch.cuda.synchronize()
+        assert torch.equal(out, graph_spec), "graph replay and direct call differ"
     _lib.check(L.sr_timing_enable(0))
     kern_ms = ctypes.c_double(0)
     kern_n = ctypes.c_int(0)
     _lib.check(L.sr_timing_read(ctypes.byref(kern_ms), ctypes.byref(kern_n)))
-    _lib.check(L.sr_workspace_status(ctypes.c_void_p(wsp.buf.data_ptr()),
-                                     ctypes.c_void_p(stream.cuda_stream)))
-    elapsed_ms = ev0.elapsed_time(ev1)
     if dist:
         t = torch.tensor([elapsed_ms], device=device)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -538,7 +566,11 @@ def main():
                                  f"step records ({batch.total_steps * 64 / 1e6:.0f} MB) "
                                  "exceed L2",
                            "parallelism": f"replicas x{ws} (tracks independent)"},
-                "e2e": e2e, "gpu_launches": 3 * args.steps * 1,
+                "e2e": e2e, "gpu_launches": 3 * args.steps,
+                "launch": {"cuda_graph": graph is not None,
+                           "graph_nodes": (dict(zip(("kernels", "nodes"), graph.nodes()))
+                                           if graph is not None else None),
+                           "shape": shape, "autotune": tune},
                 "clocks": clk, "roofline": roofline, "cpu_baseline": cpu, "fp64_port": fp64}
         print(json.dumps(line), flush=True)
     if dist:

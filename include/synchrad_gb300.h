@@ -145,9 +145,65 @@ const char *sr_last_error(void);
 int sr_version(void);
 
 /* ---------------------------------------------------------------------------
+ * Work shape autotuning and CUDA graphs.  No counterpart in the reference
+ * (its host loop launches one OpenCL kernel per track, synchrad/calc.py:257-267).
+ * ------------------------------------------------------------------------- */
+
+/* Work shape of the persistent mixed-precision launch. */
+typedef struct sr_config {
+  int32_t points_per_lane;      /* omega points each lane carries (far: 8..32) */
+  int32_t lanes_per_direction;  /* lanes sharing one direction's omega axis */
+  int32_t steps_per_stage;      /* step records per TMA stage (far field) */
+  int32_t track_subsets;        /* tracks are split into this many subsets */
+  int32_t ctas;                 /* CTAs of the persistent launch */
+  int32_t reserved;
+  double ms;                    /* time on the tuning sample (0: not timed) */
+} sr_config;
+
+/* Times candidate work shapes (points per lane and lanes per direction, then
+ * steps per stage, then track subsets) with CUDA events on a sample of the
+ * problem (its leading tracks, about budget_ms / 100 of work each run) and
+ * caches the fastest for problems of exactly these sizes; later sr_spectrum
+ * and sr_workspace_bytes calls for such problems use it (query the workspace
+ * size after tuning).  Allocates and frees its own scratch; stops starting new
+ * candidates once budget_ms (<= 0: 3000) has passed.  best / dflt (either may
+ * be NULL) receive the chosen and the default shape with their sample times.
+ * SR_PREC_MIXED only. */
+int sr_autotune(const sr_tracks *tracks, const sr_grid *grid, int comp, int precision,
+                double budget_ms, void *stream, sr_config *best, sr_config *dflt);
+
+/* The work shape sr_spectrum uses for this problem (tuned or default). */
+int sr_config_get(const sr_tracks *tracks, const sr_grid *grid, int comp, int precision,
+                  sr_config *out);
+
+/* Pins a work shape for problems of exactly these sizes (for instance one
+ * tuned in an earlier process): points_per_lane (far 8/16/24/32, near 8),
+ * lanes_per_direction (8/16/32), steps_per_stage (far: multiple of 32 in
+ * [32, 512]) and track_subsets (0: default, at most 64) are used, the rest is
+ * derived. */
+int sr_config_set(const sr_tracks *tracks, const sr_grid *grid, int comp, int precision,
+                  const sr_config *config);
+
+/* Forgets every tuned work shape. */
+int sr_config_clear(void);
+
+/* One sr_spectrum call (all its copies and kernels) captured into a CUDA graph
+ * on a private stream and instantiated; sr_graph_launch replays it on any
+ * stream, accumulating into the same `out` from the same device buffers (the
+ * track, grid, output and workspace pointers are baked in). */
+typedef struct sr_graph sr_graph;
+int sr_graph_create(const sr_tracks *tracks, const sr_grid *grid, int comp, int precision,
+                    void *const *out, void *workspace, size_t workspace_bytes,
+                    sr_graph **graph);
+int sr_graph_launch(sr_graph *graph, void *stream);
+/* Kernel nodes and all nodes of the captured graph. */
+int sr_graph_nodes(const sr_graph *graph, int *n_kernels, int *n_nodes);
+void sr_graph_destroy(sr_graph *graph);
+
+/* ---------------------------------------------------------------------------
  * Adjoint of the mixed-precision far field, comp 'total', one snapshot.
  * No counterpart in the reference (it has no gradients).  The |dphase| < pi
- * mask is held fixed; the omega axis must be uniform.
+ * mask is held fixed; uniform and non-uniform omega axes.
  * ------------------------------------------------------------------------- */
 
 /* sr_spectrum (SR_PREC_MIXED, far, SR_COMP_TOTAL, n_snaps = 1) that also

@@ -28,6 +28,7 @@ SOURCES = {
     "sr_far_adjoint.cu": [],
     "sr_diag.cu": [],
     "sr_noalloc.cu": [],
+    "sr_tune.cu": [],
 }
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",

@@ -84,6 +84,22 @@ class SrGrid(ctypes.Structure):
 
 
 # Exported symbols of include/synchrad_gb300.h (checked by the CPU tests).
+class SrConfig(ctypes.Structure):
+    """sr_config: work shape of the persistent mixed-precision launch."""
+    _fields_ = [
+        ("points_per_lane", ctypes.c_int32),
+        ("lanes_per_direction", ctypes.c_int32),
+        ("steps_per_stage", ctypes.c_int32),
+        ("track_subsets", ctypes.c_int32),
+        ("ctas", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("ms", ctypes.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
 EXPORTS = (
     "sr_spectrum", "sr_workspace_bytes", "sr_workspace_status", "sr_last_error",
     "sr_version", "sr_far_total", "sr_far_cartesian_comps",
@@ -92,6 +108,8 @@ EXPORTS = (
     "sr_near_cartesian_comps_complex", "sr_timing_enable", "sr_timing_read",
     "sr_probe_fp32_peak", "sr_spectrum_noalloc", "sr_far_total_forward_saved",
     "sr_far_total_backward_workspace_bytes", "sr_far_total_backward",
+    "sr_autotune", "sr_config_get", "sr_config_set", "sr_config_clear", "sr_graph_create", "sr_graph_launch",
+    "sr_graph_nodes", "sr_graph_destroy",
 )
 
 _lock = threading.Lock()
@@ -115,6 +133,26 @@ def _declare(L: ctypes.CDLL) -> None:
     L.sr_far_total_backward.restype = i32
     L.sr_far_total_backward.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid), vp, vp,
                                         ctypes.POINTER(vp), vp, vp, ctypes.c_size_t, vp]
+    L.sr_autotune.restype = i32
+    L.sr_autotune.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid), i32, i32, dbl, vp,
+                              ctypes.POINTER(SrConfig), ctypes.POINTER(SrConfig)]
+    L.sr_config_get.restype = i32
+    L.sr_config_get.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid), i32, i32,
+                                ctypes.POINTER(SrConfig)]
+    L.sr_config_set.restype = i32
+    L.sr_config_set.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid), i32, i32,
+                                ctypes.POINTER(SrConfig)]
+    L.sr_config_clear.restype = i32
+    L.sr_config_clear.argtypes = []
+    L.sr_graph_create.restype = i32
+    L.sr_graph_create.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid), i32, i32,
+                                  ctypes.POINTER(vp), vp, ctypes.c_size_t, ctypes.POINTER(vp)]
+    L.sr_graph_launch.restype = i32
+    L.sr_graph_launch.argtypes = [vp, vp]
+    L.sr_graph_nodes.restype = i32
+    L.sr_graph_nodes.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(i32)]
+    L.sr_graph_destroy.restype = None
+    L.sr_graph_destroy.argtypes = [vp]
     L.sr_workspace_bytes.restype = ctypes.c_int64
     L.sr_workspace_bytes.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid), i32, i32]
     L.sr_workspace_status.restype = i32

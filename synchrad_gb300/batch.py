@@ -213,3 +213,95 @@ def run_spectrum(batch: TrackBatch, grid: GridDevice, comp: str, precision: int,
     _lib.check(rc)
     if check_status and ws is not None:
         _lib.check(L.sr_workspace_status(ctypes.c_void_p(ws.data_ptr()), sptr))
+
+
+def autotune(batch: TrackBatch, grid: GridDevice, comp: str = "total",
+             precision: int = _lib.SR_PREC_MIXED, budget_ms: float = 3000.0,
+             stream=None) -> dict:
+    """Tune the work shape of the persistent mixed-precision launch for this
+    batch's sizes (``sr_autotune``); later ``run_spectrum`` calls with the same
+    sizes use the choice.  Returns {'best': ..., 'default': ...} shapes with
+    their times on the tuning sample."""
+    L = _lib.lib()
+    ts, gs = batch.c_struct(), grid.c_struct()
+    best, dflt = _lib.SrConfig(), _lib.SrConfig()
+    if stream is None:
+        stream = torch.cuda.current_stream(batch.offsets.device)
+    _lib.check(L.sr_autotune(ctypes.byref(ts), ctypes.byref(gs), _lib.COMP_IDS[comp], precision,
+                             float(budget_ms), ctypes.c_void_p(stream.cuda_stream),
+                             ctypes.byref(best), ctypes.byref(dflt)))
+    return {"best": best.as_dict(), "default": dflt.as_dict()}
+
+
+def current_config(batch: TrackBatch, grid: GridDevice, comp: str = "total",
+                   precision: int = _lib.SR_PREC_MIXED) -> dict:
+    """The work shape ``run_spectrum`` uses for these sizes."""
+    L = _lib.lib()
+    ts, gs = batch.c_struct(), grid.c_struct()
+    c = _lib.SrConfig()
+    _lib.check(L.sr_config_get(ctypes.byref(ts), ctypes.byref(gs), _lib.COMP_IDS[comp],
+                               precision, ctypes.byref(c)))
+    return c.as_dict()
+
+
+def set_config(batch: TrackBatch, grid: GridDevice, comp: str = "total",
+               precision: int = _lib.SR_PREC_MIXED, points_per_lane: int = 32,
+               lanes_per_direction: int = 32, steps_per_stage: int = 128,
+               track_subsets: int = 0) -> None:
+    """Pin a work shape for this batch's sizes (``sr_config_set``)."""
+    c = _lib.SrConfig(points_per_lane, lanes_per_direction, steps_per_stage, track_subsets, 0, 0,
+                      0.0)
+    ts, gs = batch.c_struct(), grid.c_struct()
+    _lib.check(_lib.lib().sr_config_set(ctypes.byref(ts), ctypes.byref(gs), _lib.COMP_IDS[comp],
+                                        precision, ctypes.byref(c)))
+
+
+class SpectrumGraph:
+    """One ``sr_spectrum`` call captured as a CUDA graph (``sr_graph_create``)
+    and replayed by ``launch``; the batch, grid, outputs and workspace must stay
+    alive and in place while the graph is used."""
+
+    def __init__(self, batch: TrackBatch, grid: GridDevice, comp: str, precision: int,
+                 outputs: list, workspace: Workspace | None = None):
+        L = _lib.lib()
+        cid = _lib.COMP_IDS[comp]
+        if len(outputs) != _lib.N_OUT[cid]:
+            raise ValueError(f"comp {comp!r} needs {_lib.N_OUT[cid]} output arrays")
+        ts, gs = batch.c_struct(), grid.c_struct()
+        need = L.sr_workspace_bytes(ctypes.byref(ts), ctypes.byref(gs), cid, precision)
+        if need < 0:
+            _lib.check(_lib.SR_ERR_INVALID)
+        self.workspace = workspace or Workspace(outputs[0].device)
+        ws = self.workspace.get(int(need))
+        outs = (ctypes.c_void_p * 6)(*([o.data_ptr() for o in outputs]
+                                       + [None] * (6 - len(outputs))))
+        h = ctypes.c_void_p()
+        _lib.check(L.sr_graph_create(ctypes.byref(ts), ctypes.byref(gs), cid, precision, outs,
+                                     ws.data_ptr() if ws is not None else None,
+                                     ctypes.c_size_t(int(need) if ws is not None else 0),
+                                     ctypes.byref(h)))
+        self._keep = (batch, grid, outputs, ws)
+        self.handle = h
+
+    def launch(self, stream=None) -> None:
+        if self.handle is None:
+            raise RuntimeError("graph destroyed")
+        if stream is None:
+            stream = torch.cuda.current_stream(self._keep[2][0].device)
+        _lib.check(_lib.lib().sr_graph_launch(self.handle, ctypes.c_void_p(stream.cuda_stream)))
+
+    def nodes(self) -> tuple:
+        k, n = ctypes.c_int(0), ctypes.c_int(0)
+        _lib.check(_lib.lib().sr_graph_nodes(self.handle, ctypes.byref(k), ctypes.byref(n)))
+        return k.value, n.value
+
+    def close(self) -> None:
+        if self.handle is not None:
+            _lib.lib().sr_graph_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

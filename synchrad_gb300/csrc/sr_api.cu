@@ -137,13 +137,9 @@ extern "C" int64_t sr_workspace_bytes(const sr_tracks *t, const sr_grid *g, int 
   const int nout = n_outputs(comp);
   if (nout == 0) return -1;
   const uint64_t P = (uint64_t)g->n_omega * g->n_theta * g->n_phi;
-  if (g->mode == SR_MODE_FAR) {
-    const FarMixedConfig cfg =
-        far_mixed_choose(g->n_omega, g->n_theta * g->n_phi, t->n_tracks, n_sm_of_current_device());
+  const FarMixedConfig cfg = mixed_config(t, g, comp);
+  if (g->mode == SR_MODE_FAR)
     return (int64_t)far_mixed_workspace(t->total_steps, P, nout, t->n_snaps ? t->n_snaps : 1, cfg);
-  }
-  const FarMixedConfig cfg =
-      near_mixed_choose(g->n_omega, g->n_theta * g->n_phi, t->n_tracks, n_sm_of_current_device());
   return (int64_t)near_mixed_workspace(t->total_steps, P, nout, t->n_snaps ? t->n_snaps : 1, cfg);
 }
 
@@ -171,14 +167,10 @@ extern "C" int sr_spectrum(const sr_tracks *t, const sr_grid *g, int comp, int p
   cudaStream_t s = (cudaStream_t)stream;
 
   if (precision == SR_PREC_MIXED) {
-    if (g->mode == SR_MODE_FAR) {
-      const FarMixedConfig cfg = far_mixed_choose(g->n_omega, g->n_theta * g->n_phi,
-                                                  t->n_tracks, n_sm_of_current_device());
+    const FarMixedConfig cfg = mixed_config(t, g, comp);
+    if (g->mode == SR_MODE_FAR)
       return launch_far_mixed(far_mixed_params(t, g, comp, out), cfg, workspace,
                               workspace_bytes, s);
-    }
-    const FarMixedConfig cfg = near_mixed_choose(g->n_omega, g->n_theta * g->n_phi,
-                                                 t->n_tracks, n_sm_of_current_device());
     return launch_near_mixed(far_mixed_params(t, g, comp, out), cfg, workspace,
                              workspace_bytes, s);
   }

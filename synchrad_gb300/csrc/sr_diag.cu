@@ -24,6 +24,9 @@ bool timing_enabled() {
 void timing_record(cudaStream_t s, bool start, void **token) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (!g_timing) return;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone)
+    return;  // kernels inside a captured graph are not timed one by one
   cudaEvent_t e;
   if (cudaEventCreate(&e) != cudaSuccess) return;
   cudaEventRecord(e, s);

@@ -560,8 +560,7 @@ extern "C" int sr_far_total_forward_saved(const sr_tracks *t, const sr_grid *g, 
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e = cudaMemsetAsync(saved_A, 0, (size_t)t->n_tracks * P * 16, s);
   if (e != cudaSuccess) return cuda_fail(e, "saved_A reset");
-  const FarMixedConfig cfg = far_mixed_choose(g->n_omega, g->n_theta * g->n_phi, t->n_tracks,
-                                              device_sm_count());
+  const FarMixedConfig cfg = mixed_config(t, g, SR_COMP_TOTAL);
   FarMixedParams p = make_far_mixed_params(t, g, SR_COMP_TOTAL, out);
   p.save_A = saved_A;
   return launch_far_mixed(p, cfg, workspace, workspace_bytes, s);

@@ -118,11 +118,11 @@ constexpr int kMaxDpw = 4;  // directions per warp (omega tiles narrower than 32
 
 template <int W>
 struct SmemFixed {
-  float4 stage[2][kStage * kRecF4];  // 2 x 8 KB of step records
   uint64_t bar[2];
   uint64_t pad_[2];
   DirConst dc[W][kMaxDpw];
-  // followed by float4 setup[W][32][dpw][6]
+  // followed by float4 setup[W][32][dpw][6], then the two stage buffers of
+  // p.stage_steps step records each
 };
 
 // Kernel of the mixed-precision far field.  K points per lane (two packed
@@ -137,6 +137,10 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int dsub = lane / L, ll = lane % L;
   float4 *setup = setup_all + (size_t)warp * 32 * dpw * 6;
+  const uint32_t S = p.stage_steps;  // steps per TMA stage
+  float4 *stage_buf[2];
+  stage_buf[0] = setup_all + (size_t)W * 32 * dpw * 6;
+  stage_buf[1] = stage_buf[0] + (size_t)S * kRecF4;
   constexpr int KP = K / 2, HP = KP / 2;
 
   if (threadIdx.x == 0) {
@@ -212,11 +216,11 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
     uint32_t cur_t = t0;
     while (cur_t < t1 && track_body(p, cur_t) == 0) ++cur_t;
     if (threadIdx.x == 0 && cur_t < t1) {
-      const uint32_t cnt = min((uint32_t)kStage, track_body(p, cur_t));
+      const uint32_t cnt = min(S, track_body(p, cur_t));
       const int b = stage_no & 1;
       fence_proxy_async();
       mbar_arrive_expect_tx(&sm.bar[b], cnt * 64u);
-      bulk_g2s(sm.stage[b], p.records + (p.offsets[cur_t]) * kRecF4, cnt * 64u, &sm.bar[b]);
+      bulk_g2s(stage_buf[b], p.records + (p.offsets[cur_t]) * kRecF4, cnt * 64u, &sm.bar[b]);
     }
 
     for (uint32_t t = t0; t < t1; ++t) {
@@ -322,23 +326,23 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
       };
 
       uint32_t stage_in_track = 0;
-      for (uint32_t s0 = 0; s0 < n_body; s0 += kStage, ++stage_in_track) {
-        const uint32_t cnt = min((uint32_t)kStage, n_body - s0);
+      for (uint32_t s0 = 0; s0 < n_body; s0 += S, ++stage_in_track) {
+        const uint32_t cnt = min(S, n_body - s0);
         const int b = stage_no & 1;
         // Issue the next stage (this track or the next non-empty one of the item).
         if (threadIdx.x == 0) {
-          uint32_t nt = t, ns0 = s0 + kStage;
+          uint32_t nt = t, ns0 = s0 + S;
           if (ns0 >= n_body) {
             nt = t + 1;
             ns0 = 0;
             while (nt < t1 && track_body(p, nt) == 0) ++nt;
           }
           if (nt < t1) {
-            const uint32_t ncnt = min((uint32_t)kStage, track_body(p, nt) - ns0);
+            const uint32_t ncnt = min(S, track_body(p, nt) - ns0);
             const int nbuf = (stage_no + 1) & 1;
             fence_proxy_async();
             mbar_arrive_expect_tx(&sm.bar[nbuf], ncnt * 64u);
-            bulk_g2s(sm.stage[nbuf], p.records + (p.offsets[nt] + ns0) * kRecF4, ncnt * 64u,
+            bulk_g2s(stage_buf[nbuf], p.records + (p.offsets[nt] + ns0) * kRecF4, ncnt * 64u,
                      &sm.bar[nbuf]);
           }
         }
@@ -353,7 +357,7 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
           __syncthreads();
           return;
         }
-        const float4 *stg = sm.stage[b];
+        const float4 *stg = stage_buf[b];
 
         if (active_w) {
           for (uint32_t c0 = 0; c0 < cnt; c0 += 32) {
@@ -567,7 +571,7 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
             __syncwarp();
           }
           // ---- fold the FP32 sums into the compensated pairs every few stages ----
-          if ((stage_in_track + 1) % kFoldStages == 0) fold();
+          if ((stage_in_track + 1) % p.fold_stages == 0) fold();
         } else {
           // inactive warp: keep the snapshot state in step with the others
           for (uint32_t i = 0; i < cnt; ++i) {
@@ -593,13 +597,14 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
 
 constexpr int kW = 8;  // warps per CTA
 
-size_t smem_bytes(int dpw) {
-  return sizeof(SmemFixed<kW>) + (size_t)kW * 32 * dpw * 6 * sizeof(float4);
+size_t smem_bytes(int dpw, int stage) {
+  return sizeof(SmemFixed<kW>) + (size_t)kW * 32 * dpw * 6 * sizeof(float4) +
+         (size_t)2 * stage * kRecF4 * sizeof(float4);
 }
 
 template <int K>
 int launch_main(const FarMixedParams &p, int grid, cudaStream_t s) {
-  const size_t smem = smem_bytes((int)p.dpw);
+  const size_t smem = smem_bytes((int)p.dpw, (int)p.stage_steps);
   cudaError_t e = cudaFuncSetAttribute(far_mixed_kernel<K, kW>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_fail(e, "far_mixed smem attribute");
@@ -627,26 +632,24 @@ void launch_far_prepass(const FarMixedParams &p, int blocks, cudaStream_t stream
     far_prepass_kernel<double><<<blocks, 256, 0, stream>>>(p);
 }
 
-// Work shape: K points per lane and L lanes per direction (32/L directions per
-// warp).  The widest lane chunk (K = 32) amortises the per-step reseed best;
-// narrower omega axes put several directions in one warp.
-FarMixedConfig far_mixed_choose(uint32_t n_omega, uint32_t n_dirs, uint32_t n_tracks,
-                                int n_sm) {
+// A complete configuration from its free parameters: K points per lane, L
+// lanes per direction (32/L directions per warp), steps per stage and track
+// subsets (0: enough subsets for about 16 work items per SM).
+FarMixedConfig far_mixed_make(uint32_t n_omega, uint32_t n_dirs, uint32_t n_tracks, int n_sm,
+                              int K, int L, int stage, int n_sub) {
   FarMixedConfig c;
   c.W = kW;
   c.ctas_per_sm = 1;
-  c.K = 32;
-  int L = 32;
-  while (L > 32 / kMaxDpw && (uint32_t)(L / 2) * 32u >= n_omega) L /= 2;
-  // narrow axes: shrink K while the lanes of a direction would idle
-  while (c.K > 8 && (uint32_t)(L * (c.K - 8)) >= n_omega) c.K -= 8;
+  c.K = K;
   c.L = L;
   c.dpw = 32 / L;
-  const uint64_t n_wtiles = (n_omega + (uint64_t)L * c.K - 1) / ((uint64_t)L * c.K);
+  c.stage = stage;
+  const uint64_t n_wtiles = (n_omega + (uint64_t)L * K - 1) / ((uint64_t)L * K);
   const uint64_t dgroups = (n_dirs + c.dpw - 1) / c.dpw;
   const uint64_t groups = (dgroups * n_wtiles + c.W - 1) / c.W;
   const uint64_t capacity = (uint64_t)n_sm * c.ctas_per_sm;
-  uint64_t nsub = (16 * capacity + groups - 1) / (groups ? groups : 1);
+  uint64_t nsub = n_sub > 0 ? (uint64_t)n_sub
+                            : (16 * capacity + groups - 1) / (groups ? groups : 1);
   if (nsub > n_tracks) nsub = n_tracks;
   if (nsub < 1) nsub = 1;
   if (nsub > 64) nsub = 64;
@@ -654,6 +657,17 @@ FarMixedConfig far_mixed_choose(uint32_t n_omega, uint32_t n_dirs, uint32_t n_tr
   c.grid = (int)std::min<uint64_t>(groups * nsub, capacity);
   if (c.grid < 1) c.grid = 1;
   return c;
+}
+
+// Default work shape: the widest lane chunk (K = 32) amortises the per-step
+// reseed best; narrower omega axes put several directions in one warp and
+// shrink K while the lanes of a direction would idle.
+FarMixedConfig far_mixed_choose(uint32_t n_omega, uint32_t n_dirs, uint32_t n_tracks,
+                                int n_sm) {
+  int K = 32, L = 32;
+  while (L > 32 / kMaxDpw && (uint32_t)(L / 2) * 32u >= n_omega) L /= 2;
+  while (K > 8 && (uint32_t)(L * (K - 8)) >= n_omega) K -= 8;
+  return far_mixed_make(n_omega, n_dirs, n_tracks, n_sm, K, L, kStage, 0);
 }
 
 size_t far_mixed_workspace(int64_t total_steps, uint64_t n_points, int n_out, uint32_t n_snaps,
@@ -688,6 +702,10 @@ int launch_far_mixed(FarMixedParams p, const FarMixedConfig &cfg, void *ws, size
   p.n_groups = (uint32_t)(((uint64_t)dgroups * p.n_wtiles + cfg.W - 1) / cfg.W);
   p.n_sub = (uint32_t)cfg.n_sub;
   p.n_items = p.n_groups * p.n_sub;
+  if (cfg.stage < 32 || cfg.stage > 512 || (cfg.stage & 31) != 0)
+    return fail(SR_ERR_INVALID, "steps per stage %d (multiples of 32 in [32, 512])", cfg.stage);
+  p.stage_steps = (uint32_t)cfg.stage;
+  p.fold_stages = (uint32_t)std::max(1, 1024 / cfg.stage);  // fold about every 1024 steps
 
   cudaError_t e = cudaMemsetAsync(w, 0, 256, stream);
   if (e != cudaSuccess) return cuda_fail(e, "status reset");

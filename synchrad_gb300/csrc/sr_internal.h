@@ -59,6 +59,8 @@ struct FarMixedParams {
   uint32_t n_sub;      // track subsets
   uint32_t n_items;    // n_groups * n_sub
   uint32_t dpw;        // directions per warp
+  uint32_t stage_steps;  // far field: step records per TMA stage
+  uint32_t fold_stages;  // far field: stages between folds of the FP32 sums
   // workspace
   float4 *records;     // [total_steps][4]
   double *partial;     // [n_sub][n_out][n_snaps][P]
@@ -77,8 +79,16 @@ struct FarMixedConfig {
   int n_sub;    // track subsets
   int ctas_per_sm;
   int grid;     // CTAs of the persistent launch
+  int stage;    // step records per TMA stage (far field; multiple of 32, <= 512)
 };
 
+FarMixedConfig far_mixed_make(uint32_t n_omega, uint32_t n_dirs, uint32_t n_tracks, int n_sm,
+                              int K, int L, int stage, int n_sub);
+FarMixedConfig near_mixed_make(uint32_t n_omega, uint32_t n_screen, uint32_t n_tracks, int n_sm,
+                               int L, int n_sub);
+// The configuration sr_spectrum uses for a mixed-precision problem: the
+// autotuner's choice when one is cached for this problem, else the default.
+FarMixedConfig mixed_config(const sr_tracks *t, const sr_grid *g, int comp);
 FarMixedConfig far_mixed_choose(uint32_t n_omega, uint32_t n_dirs,
                                 uint32_t n_tracks, int n_sm);
 size_t far_mixed_workspace(int64_t total_steps, uint64_t n_points, int n_out,

@@ -552,21 +552,23 @@ size_t near_smem_bytes(int dpw) {
 
 }  // namespace
 
-FarMixedConfig near_mixed_choose(uint32_t n_omega, uint32_t n_screen, uint32_t n_tracks,
-                                 int n_sm) {
+// A complete configuration from L lanes per direction and the track subsets
+// (0: enough subsets for about 16 work items per SM); K is fixed.
+FarMixedConfig near_mixed_make(uint32_t n_omega, uint32_t n_screen, uint32_t n_tracks, int n_sm,
+                               int L, int n_sub) {
   FarMixedConfig c;
   c.W = kNW;
   c.ctas_per_sm = 1;
   c.K = kNK;
-  int L = 32;
-  while (L > 32 / kNMaxDpw && (uint32_t)(L / 2) * kNK >= n_omega) L /= 2;
+  c.stage = kStage;
   c.L = L;
   c.dpw = 32 / L;
   const uint64_t n_wtiles = (n_omega + (uint64_t)L * c.K - 1) / ((uint64_t)L * c.K);
   const uint64_t dgroups = (n_screen + c.dpw - 1) / c.dpw;
   const uint64_t groups = (dgroups * n_wtiles + c.W - 1) / c.W;
   const uint64_t capacity = (uint64_t)n_sm * c.ctas_per_sm;
-  uint64_t nsub = (16 * capacity + groups - 1) / (groups ? groups : 1);
+  uint64_t nsub = n_sub > 0 ? (uint64_t)n_sub
+                            : (16 * capacity + groups - 1) / (groups ? groups : 1);
   if (nsub > n_tracks) nsub = n_tracks;
   if (nsub < 1) nsub = 1;
   if (nsub > 64) nsub = 64;
@@ -574,6 +576,13 @@ FarMixedConfig near_mixed_choose(uint32_t n_omega, uint32_t n_screen, uint32_t n
   c.grid = (int)std::min<uint64_t>(groups * nsub, capacity);
   if (c.grid < 1) c.grid = 1;
   return c;
+}
+
+FarMixedConfig near_mixed_choose(uint32_t n_omega, uint32_t n_screen, uint32_t n_tracks,
+                                 int n_sm) {
+  int L = 32;
+  while (L > 32 / kNMaxDpw && (uint32_t)(L / 2) * kNK >= n_omega) L /= 2;
+  return near_mixed_make(n_omega, n_screen, n_tracks, n_sm, L, 0);
 }
 
 size_t near_mixed_workspace(int64_t total_steps, uint64_t n_points, int n_out, uint32_t n_snaps,

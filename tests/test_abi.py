@@ -11,7 +11,8 @@ ROOT = Path(__file__).resolve().parents[1]
 
 def declared_entry_points():
     text = (ROOT / "include" / "synchrad_gb300.h").read_text()
-    return sorted(set(re.findall(r"^\s*(?:int|int64_t|const char \*)\s*(sr_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t|void|const char \*)\s*(sr_\w+)\s*\(",
+                                 text, re.M)))
 
 
 def test_header_declares_the_binding_table():
