@@ -42,6 +42,7 @@ METRIC = "Gpt·steps/s (spectral pts × track steps), mixed vs FP64 at ≤1e-5 r
 UNIT = "Gpt·steps/s"
 FLOPS_PER_UNIT = 14      # far field, mixed: 2 FMUL + 6 FFMA per point-step
 ADJ_FLOPS_PER_UNIT = 22  # far adjoint: 8 FFMA (E and F sums) + 1 FMUL + 2 FFMA (rotation)
+NEAR_ADJ_FLOPS_PER_UNIT = 42  # near adjoint: 18 FFMA (R0, I1, R2 x 3) + rotation
 CANONICAL_FLOPS = 18     # the 3-component formulation's count
 
 
@@ -51,7 +52,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="far", choices=["far", "near", "ragged", "adjoint"],
+    ap.add_argument("--workload", default="far", choices=["far", "near", "ragged", "adjoint", "near-adjoint"],
                     help="far: the headline configuration (default); near: 2048 helical "
                          "tracks on a screen at 20 undulator lengths; ragged: 8192 FP32 "
                          "betatron tracks of 500-20000 steps; adjoint: forward and "
@@ -150,6 +151,10 @@ def make_workload(args):
         if args.track_steps is not None:
             kw["n_steps"] = args.track_steps
         return wl.c4_adjoint(**kw)
+    if args.workload == "near-adjoint":
+        if args.track_steps is not None:
+            kw["n_steps"] = args.track_steps
+        return wl.c5_near_helical(**kw)
     if args.track_steps is not None:
         kw["steps_range"] = (max(2, args.track_steps // 40), args.track_steps)
     return wl.c3_betatron_ragged(**kw)
@@ -225,11 +230,16 @@ def adjoint_main(args):
     L = sum(((S - T) / max T)^2) against a target spectrum T of the same tracks
     with seeded perturbations (x, y and momenta 1e-3 relative), computed once
     before timing.  One step = forward + loss + backward, L2 flushed before
-    each.  Reports the forward and backward times and their ratio."""
+    each.  Reports the forward and backward times and their ratio.
+
+    ``--workload near-adjoint``: the near-field workload (screen at 20
+    undulator lengths) with the on-screen energy integral of
+    Utilities.get_energy as the loss (its quadrature weights as dL/dS)."""
     import torch
     from oracle import host as ohost
     from synchrad_gb300 import _lib
-    from synchrad_gb300.autograd import far_total_spectrum, make_layout
+    from synchrad_gb300.autograd import make_layout, total_spectrum_fn
+    from synchrad_gb300.utils import Utilities
 
     ws, rank, local = dist_env()
     if ws > 1:
@@ -244,19 +254,37 @@ def adjoint_main(args):
     w = make_workload(args)
     a = ohost.init_args(dict(w.args, dtype="double"))
     nO, nT, nP = (int(v) for v in a["gridNodeNums"])
+    mode = w.args.get("mode", "far")
     lengths = [len(t[0]) for t in w.tracks]
-    layout = make_layout(lengths, w.time_step, ohost.device_axes(a), (nO, nT, nP), device)
+    layout = make_layout(lengths, w.time_step, ohost.device_axes(a), (nO, nT, nP), device,
+                         mode=mode, L_screen=w.L_screen or 0.0)
+    spectrum = total_spectrum_fn(mode)
     coords = [torch.tensor(np.concatenate([np.asarray(t[c], np.float64) for t in w.tracks]),
                            device=device, requires_grad=True) for c in range(6)]
     wt = torch.tensor([float(t[6]) for t in w.tracks], dtype=torch.float64, device=device,
                       requires_grad=True)
-    from synchrad_gb300 import workloads as wl
-    tgt = wl.perturbed_tracks(w.tracks, 1e-3, seed=1)
-    tgt_coords = [torch.tensor(np.concatenate([np.asarray(t[c], np.float64) for t in tgt]),
-                               device=device) for c in range(6)]
-    with torch.no_grad():
-        target = far_total_spectrum(*tgt_coords, wt.detach(), layout)
-    inv_scale = 1.0 / float(target.max())
+    if mode == "far":
+        from synchrad_gb300 import workloads as wl
+        tgt = wl.perturbed_tracks(w.tracks, 1e-3, seed=1)
+        tgt_coords = [torch.tensor(np.concatenate([np.asarray(t[c], np.float64) for t in tgt]),
+                                   device=device) for c in range(6)]
+        with torch.no_grad():
+            target = spectrum(*tgt_coords, wt.detach(), layout)
+        inv_scale = 1.0 / float(target.max())
+
+        def loss_of(S):
+            return (((S - target) * inv_scale) ** 2).sum()
+        loss_name = ("sum(((S - T) / max T)^2), T from the tracks with x, y and momenta "
+                     "perturbed 1e-3 relative (seed 1)")
+    else:
+        u = Utilities()
+        u.Args = dict(a, comp="total")
+        q = torch.tensor(np.ascontiguousarray(u.get_energy_weights(lambda0_um=1.0)
+                                              .transpose(2, 1, 0)), device=device)
+
+        def loss_of(S):
+            return (q * S).sum()
+        loss_name = "on-screen radiated energy (Utilities.get_energy quadrature, lambda0 1 um)"
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
     stream = torch.cuda.current_stream(device)
     pt_steps = w.pt_steps
@@ -267,11 +295,11 @@ def adjoint_main(args):
             c.grad = None
         if ev:
             ev[0].record(stream)
-        S = far_total_spectrum(*coords, wt, layout)
+        S = spectrum(*coords, wt, layout)
         if ev:
             ev[1].record(stream)
             _lib.check(L.sr_timing_enable(1))
-        loss = (((S - target) * inv_scale) ** 2).sum()
+        loss = loss_of(S)
         loss.backward()
         if ev:
             _lib.check(L.sr_timing_enable(0))
@@ -316,10 +344,14 @@ def adjoint_main(args):
                                     ctypes.c_void_p(stream.cuda_stream)))
     peak = max(tf_s.value, tf_p.value)
     kern_avg = kern_ms.value / max(kern_n.value, 1)
-    achieved = pt_steps * ADJ_FLOPS_PER_UNIT / (kern_avg * 1e-3) / 1e12
+    fpu = ADJ_FLOPS_PER_UNIT if mode == "far" else NEAR_ADJ_FLOPS_PER_UNIT
+    kname = "adj_far_kernel" if mode == "far" else "nadj_kernel"
+    achieved = pt_steps * fpu / (kern_avg * 1e-3) / 1e12
     if rank == 0:
-        line = {"metric": "Gpt·steps/s through forward + backward of a spectrum misfit loss "
-                          "(far field)",
+        line = {"metric": ("Gpt·steps/s through forward + backward of a spectrum misfit loss "
+                           "(far field)" if mode == "far" else
+                           "Gpt·steps/s through forward + backward of the on-screen energy "
+                           "(near field)"),
                 "value": pt_steps * ws * args.steps / (elapsed * 1e-3) / 1e9, "unit": UNIT,
                 "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -329,19 +361,18 @@ def adjoint_main(args):
                 "config": {"workload": w.name, "n_tracks": len(w.tracks),
                            "steps_per_track": int(lengths[0]), "grid": [nO, nT, nP],
                            "pt_steps_per_step": pt_steps,
-                           "loss": "sum(((S - T) / max T)^2), T from the tracks with x, y and "
-                                   "momenta perturbed 1e-3 relative (seed 1)",
+                           "loss": loss_name,
                            "l2": "flushed before every timed step (256 MB write, counted)",
                            "parallelism": f"replicas x{ws} (tracks independent)"},
                 "adjoint": {"forward_ms": fwd_ms, "backward_ms": bwd_ms,
                             "backward_over_forward": bwd_ms / fwd_ms,
-                            "adj_far_kernel_ms": kern_avg},
-                "e2e": None, "gpu_launches": 8 * args.steps,
+                            "adjoint_kernel_ms": kern_avg},
+                "e2e": None, "gpu_launches": 10 * args.steps,
                 "clocks": clocks.summary(),
                 "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak,
                              "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
-                             "traffic": None, "kernel": "adj_far_kernel",
-                             "flops_per_unit": ADJ_FLOPS_PER_UNIT,
+                             "traffic": None, "kernel": kname,
+                             "flops_per_unit": fpu,
                              "peak_source": "measured on this GPU by sr_probe_fp32_peak"},
                 "cpu_baseline": None}
         print(json.dumps(line), flush=True)
@@ -354,7 +385,7 @@ def main():
     if args.impl == "reference":
         reference_arm(args)
         return
-    if args.workload == "adjoint":
+    if args.workload in ("adjoint", "near-adjoint"):
         adjoint_main(args)
         return
     import torch

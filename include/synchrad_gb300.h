@@ -228,6 +228,22 @@ int sr_far_total_backward(const sr_tracks *tracks, const sr_grid *grid,
                           void *workspace, size_t workspace_bytes, void *stream);
 
 /* ---------------------------------------------------------------------------
+ * Adjoint of the mixed-precision near field (screen at distance L), comp
+ * 'total', one snapshot.  No counterpart in the reference.  Same conventions
+ * as the far-field adjoint above; saved_A is [n_tracks][P][8] float
+ * (A_x, A_y, A_z as re, im pairs, then two floats of padding).
+ * ------------------------------------------------------------------------- */
+int sr_near_total_forward_saved(const sr_tracks *tracks, const sr_grid *grid,
+                                double *spectrum, float *saved_A, void *workspace,
+                                size_t workspace_bytes, void *stream);
+int64_t sr_near_total_backward_workspace_bytes(const sr_tracks *tracks,
+                                               const sr_grid *grid);
+int sr_near_total_backward(const sr_tracks *tracks, const sr_grid *grid,
+                           const double *grad_spectrum, const float *saved_A,
+                           double *const *grad_track, double *grad_weight,
+                           void *workspace, size_t workspace_bytes, void *stream);
+
+/* ---------------------------------------------------------------------------
  * Diagnostics.  These have no counterpart in the reference; the benchmark uses
  * them for its roofline figures.
  * ------------------------------------------------------------------------- */

@@ -29,6 +29,7 @@ SOURCES = {
     "sr_diag.cu": [],
     "sr_noalloc.cu": [],
     "sr_tune.cu": [],
+    "sr_near_adjoint.cu": [],
 }
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",

@@ -109,7 +109,8 @@ EXPORTS = (
     "sr_probe_fp32_peak", "sr_spectrum_noalloc", "sr_far_total_forward_saved",
     "sr_far_total_backward_workspace_bytes", "sr_far_total_backward",
     "sr_autotune", "sr_config_get", "sr_config_set", "sr_config_clear", "sr_graph_create", "sr_graph_launch",
-    "sr_graph_nodes", "sr_graph_destroy",
+    "sr_graph_nodes", "sr_graph_destroy", "sr_near_total_forward_saved",
+    "sr_near_total_backward_workspace_bytes", "sr_near_total_backward",
 )
 
 _lock = threading.Lock()
@@ -153,6 +154,18 @@ def _declare(L: ctypes.CDLL) -> None:
     L.sr_graph_nodes.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(i32)]
     L.sr_graph_destroy.restype = None
     L.sr_graph_destroy.argtypes = [vp]
+    for kind in ("near",):
+        fs = getattr(L, f"sr_{kind}_total_forward_saved")
+        fs.restype = i32
+        fs.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid), vp, vp, vp,
+                       ctypes.c_size_t, vp]
+        wb = getattr(L, f"sr_{kind}_total_backward_workspace_bytes")
+        wb.restype = ctypes.c_int64
+        wb.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid)]
+        bw = getattr(L, f"sr_{kind}_total_backward")
+        bw.restype = i32
+        bw.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid), vp, vp,
+                       ctypes.POINTER(vp), vp, vp, ctypes.c_size_t, vp]
     L.sr_workspace_bytes.restype = ctypes.c_int64
     L.sr_workspace_bytes.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid), i32, i32]
     L.sr_workspace_status.restype = i32

@@ -1,16 +1,17 @@
-"""Differentiable far-field spectrum: ``torch.autograd.Function`` over the
-hand-written adjoint kernel.
+"""Differentiable spectra: ``torch.autograd.Function`` over the hand-written
+adjoint kernels.
 
-``far_total_spectrum(x, y, z, ux, uy, uz, w, layout)`` returns the
-mixed-precision far-field spectrum ``S`` (comp 'total', one snapshot, device
-layout ``[nPhi, nTheta, nOmega]``) of a batch of tracks given as concatenated
-float64 CUDA tensors (CSR order of ``layout.offsets``); its backward calls
-``sr_far_total_backward`` and returns dL/dx .. dL/duz (per step) and dL/dw
-(per track).  The |dphase| < pi mask of the reference is held fixed (it is a
-step function of the coordinates).
+``far_total_spectrum(x, y, z, ux, uy, uz, w, layout)`` and
+``near_total_spectrum(...)`` return the mixed-precision far-field or near-field
+(screen) spectrum ``S`` (comp 'total', one snapshot, device layout
+``[nPhi, nTheta|nR, nOmega]``) of a batch of tracks given as concatenated
+float64 CUDA tensors (CSR order of ``layout.offsets``); the backward calls
+``sr_far_total_backward`` / ``sr_near_total_backward`` and returns dL/dx ..
+dL/duz (per step) and dL/dw (per track).  The |dphase| < pi mask of the
+reference is held fixed (it is a step function of the coordinates).
 
-The reference has no gradients; this is an extension of its far-field
-integral (``synchrad/kernel_farfield.cl:59-107``).
+The reference has no gradients; these extend its integrals
+(``synchrad/kernel_farfield.cl:59-107``, ``synchrad/kernel_nearfield.cl:58-102``).
 """
 from __future__ import annotations
 
@@ -25,7 +26,7 @@ from .batch import GridDevice, TrackBatch, Workspace, make_grid, snap_iterations
 
 
 @dataclass
-class FarLayout:
+class SpectrumLayout:
     """Everything of a batch that is not differentiated."""
     offsets: torch.Tensor        # int64 [n+1] on the device
     it_start: torch.Tensor       # int32 [n]
@@ -34,6 +35,7 @@ class FarLayout:
     dt: float
     grid: GridDevice
     workspace: Workspace
+    mode: str = "far"
 
     @property
     def n_tracks(self) -> int:
@@ -44,9 +46,15 @@ class FarLayout:
         return int(np.prod(self.grid.n))
 
 
-def make_layout(lengths, dt, host_axes, n, device="cuda") -> FarLayout:
+FarLayout = SpectrumLayout
+
+
+def make_layout(lengths, dt, host_axes, n, device="cuda", mode="far",
+                L_screen=0.0) -> SpectrumLayout:
     """Layout for tracks of the given lengths with the reference's per-track
-    rules (it_start = 0, itEnd = length, one snapshot at the last step)."""
+    rules (it_start = 0, itEnd = length, one snapshot at the last step).
+    host_axes: far (omega2pi, sinT, cosT, sinP, cosP), near (omega2pi, R,
+    sinP, cosP) as from ``synchrad/calc.py:486-512``."""
     device = torch.device(device)
     lengths = np.asarray(lengths, dtype=np.int64)
     if np.any(lengths < 1):
@@ -55,11 +63,11 @@ def make_layout(lengths, dt, host_axes, n, device="cuda") -> FarLayout:
     np.cumsum(lengths, out=offsets[1:])
     snaps = np.concatenate([snap_iterations((0, int(L)), 1) for L in lengths])
     t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)
-    grid = make_grid("far", host_axes, n, torch.float64, device)
-    return FarLayout(t(offsets), t(np.zeros(lengths.size, np.int32)),
-                     t(lengths.astype(np.uint32).view(np.int32)),
-                     t(snaps.astype(np.uint32).view(np.int32)), float(dt), grid,
-                     Workspace(device))
+    grid = make_grid(mode, host_axes, n, torch.float64, device, L_screen=L_screen)
+    return SpectrumLayout(t(offsets), t(np.zeros(lengths.size, np.int32)),
+                          t(lengths.astype(np.uint32).view(np.int32)),
+                          t(snaps.astype(np.uint32).view(np.int32)), float(dt), grid,
+                          Workspace(device), mode)
 
 
 def _tracks_struct(coords, w, layout: FarLayout) -> TrackBatch:
@@ -68,9 +76,12 @@ def _tracks_struct(coords, w, layout: FarLayout) -> TrackBatch:
                       layout.dt)
 
 
-class FarTotalSpectrum(torch.autograd.Function):
+_SAVED_FLOATS = {"far": 4, "near": 8}  # per point and track
+
+
+class TotalSpectrum(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, x, y, z, ux, uy, uz, w, layout: FarLayout):
+    def forward(ctx, x, y, z, ux, uy, uz, w, layout: SpectrumLayout):
         L = _lib.lib()
         coords = [c.detach().contiguous() for c in (x, y, z, ux, uy, uz)]
         for c in coords:
@@ -82,16 +93,16 @@ class FarTotalSpectrum(torch.autograd.Function):
         nO, nT, nP = layout.grid.n
         P = layout.n_points
         spec = torch.zeros((nP, nT, nO), dtype=torch.float64, device=x.device)
-        saved = torch.empty(layout.n_tracks * P * 4, dtype=torch.float32, device=x.device)
+        saved = torch.empty(layout.n_tracks * P * _SAVED_FLOATS[layout.mode], dtype=torch.float32,
+                            device=x.device)
         need = L.sr_workspace_bytes(ctypes.byref(ts), ctypes.byref(gs), 0, _lib.SR_PREC_MIXED)
         if need < 0:
             _lib.check(_lib.SR_ERR_INVALID if need == -1 else int(need))
         ws = layout.workspace.get(max(int(need), 256))
         stream = ctypes.c_void_p(torch.cuda.current_stream(x.device).cuda_stream)
-        _lib.check(L.sr_far_total_forward_saved(ctypes.byref(ts), ctypes.byref(gs),
-                                                spec.data_ptr(), saved.data_ptr(),
-                                                ws.data_ptr(), ctypes.c_size_t(int(need)),
-                                                stream))
+        fwd = getattr(L, f"sr_{layout.mode}_total_forward_saved")
+        _lib.check(fwd(ctypes.byref(ts), ctypes.byref(gs), spec.data_ptr(), saved.data_ptr(),
+                       ws.data_ptr(), ctypes.c_size_t(int(need)), stream))
         ctx.save_for_backward(*coords, wd, saved)
         ctx.layout = layout
         return spec
@@ -106,18 +117,36 @@ class FarTotalSpectrum(torch.autograd.Function):
         g = grad_spec.detach().contiguous().to(torch.float64)
         grads = [torch.empty_like(c) for c in coords]
         gw = torch.empty(layout.n_tracks, dtype=torch.float64, device=g.device)
-        need = L.sr_far_total_backward_workspace_bytes(ctypes.byref(ts), ctypes.byref(gs))
+        need = getattr(L, f"sr_{layout.mode}_total_backward_workspace_bytes")(
+            ctypes.byref(ts), ctypes.byref(gs))
         if need < 0:
             _lib.check(_lib.SR_ERR_INVALID)
         ws = layout.workspace.get(max(int(need), 256))
         ptrs = (ctypes.c_void_p * 6)(*[t.data_ptr() for t in grads])
         stream = ctypes.c_void_p(torch.cuda.current_stream(g.device).cuda_stream)
-        _lib.check(L.sr_far_total_backward(ctypes.byref(ts), ctypes.byref(gs), g.data_ptr(),
-                                           saved.data_ptr(), ptrs, gw.data_ptr(), ws.data_ptr(),
-                                           ctypes.c_size_t(int(need)), stream))
+        bwd = getattr(L, f"sr_{layout.mode}_total_backward")
+        _lib.check(bwd(ctypes.byref(ts), ctypes.byref(gs), g.data_ptr(), saved.data_ptr(), ptrs,
+                       gw.data_ptr(), ws.data_ptr(), ctypes.c_size_t(int(need)), stream))
         return (*grads, gw, None)
 
 
-def far_total_spectrum(x, y, z, ux, uy, uz, w, layout: FarLayout) -> torch.Tensor:
+FarTotalSpectrum = TotalSpectrum
+
+
+def far_total_spectrum(x, y, z, ux, uy, uz, w, layout: SpectrumLayout) -> torch.Tensor:
     """Differentiable mixed-precision far-field spectrum (see module docstring)."""
-    return FarTotalSpectrum.apply(x, y, z, ux, uy, uz, w, layout)
+    if layout.mode != "far":
+        raise ValueError("far_total_spectrum needs a far-field layout")
+    return TotalSpectrum.apply(x, y, z, ux, uy, uz, w, layout)
+
+
+def near_total_spectrum(x, y, z, ux, uy, uz, w, layout: SpectrumLayout) -> torch.Tensor:
+    """Differentiable mixed-precision near-field (screen) spectrum."""
+    if layout.mode != "near":
+        raise ValueError("near_total_spectrum needs a near-field layout (mode='near')")
+    return TotalSpectrum.apply(x, y, z, ux, uy, uz, w, layout)
+
+
+def total_spectrum_fn(mode: str):
+    """far_total_spectrum or near_total_spectrum by mode."""
+    return {"far": far_total_spectrum, "near": near_total_spectrum}[mode]

@@ -1,0 +1,87 @@
+// Pieces shared by the far- and near-field adjoint kernels.
+#pragma once
+
+#include "sr_common.cuh"
+#include "sr_internal.h"
+#include "sr_mixed_common.cuh"
+
+namespace sr {
+namespace {
+
+struct AdjGlobals {
+  float dw_h, dw_l;        // omega spacing (rad per unit time) as a double-float
+  float w0f, dwf;          // first omega and spacing in FP32
+  float wabs_min, wabs_max;
+  int uniform;             // omega axis uniform to 1e-12
+  int pad_;
+};
+
+// Omega table, axis uniformity and |omega| range (one block).
+__global__ void adj_globals_kernel(FarMixedParams p, float4 *wtab, AdjGlobals *glob) {
+  const uint32_t nO = p.n_omega;
+  const double w0 = p.omega[0];
+  const double dw = (nO > 1) ? (p.omega[nO - 1] - w0) / (double)(nO - 1) : 0.0;
+  bool uni = true;
+  float amin = 3.0e38f, amax = 0.f;
+  for (uint32_t m = threadIdx.x; m < nO; m += blockDim.x) {
+    const double wm = p.omega[m];
+    if (fabs(wm - (w0 + (double)m * dw)) > 1e-12 * fabs(wm) + 1e-300) uni = false;
+    const df r = df_from_double(wm * 0.15915494309189533577);
+    const float aw = (float)fabs(wm);
+    wtab[m] = make_float4(r.hi, r.lo, (float)wm, aw);
+    amin = fminf(amin, aw);
+    amax = fmaxf(amax, aw);
+  }
+  __shared__ float smin[256], smax[256];
+  smin[threadIdx.x] = amin;
+  smax[threadIdx.x] = amax;
+  const int all_uni = __syncthreads_and(uni ? 1 : 0);
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) {
+      smin[threadIdx.x] = fminf(smin[threadIdx.x], smin[threadIdx.x + o]);
+      smax[threadIdx.x] = fmaxf(smax[threadIdx.x], smax[threadIdx.x + o]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    AdjGlobals g;
+    const df d = df_from_double(dw);
+    g.dw_h = d.hi;
+    g.dw_l = d.lo;
+    g.w0f = (float)w0;
+    g.dwf = (float)dw;
+    g.wabs_min = smin[0];
+    g.wabs_max = smax[0];
+    g.uniform = all_uni;
+    g.pad_ = 0;
+    *glob = g;
+  }
+}
+
+// Work items: ceil(n_body / steps_per_item) per track, as an exclusive prefix
+// (one block of 1024 threads, each scanning a contiguous run of tracks).
+__global__ void adj_items_kernel(FarMixedParams p, int64_t *item_off, uint32_t steps_per_item) {
+  const uint32_t n = p.n_tracks;
+  const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
+  const uint32_t t0 = min(n, threadIdx.x * per), t1 = min(n, t0 + per);
+  int64_t local = 0;
+  for (uint32_t t = t0; t < t1; ++t) local += (track_body(p, t) + steps_per_item - 1) / steps_per_item;
+  __shared__ int64_t sums[1024];
+  sums[threadIdx.x] = local;
+  __syncthreads();
+  for (uint32_t off = 1; off < blockDim.x; off <<= 1) {
+    const int64_t v = threadIdx.x >= off ? sums[threadIdx.x - off] : 0;
+    __syncthreads();
+    sums[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int64_t run = threadIdx.x ? sums[threadIdx.x - 1] : 0;
+  for (uint32_t t = t0; t < t1; ++t) {
+    item_off[t] = run;
+    run += (track_body(p, t) + steps_per_item - 1) / steps_per_item;
+  }
+  if (threadIdx.x == blockDim.x - 1) item_off[n] = sums[blockDim.x - 1];
+}
+
+}  // namespace
+}  // namespace sr

@@ -27,6 +27,7 @@
 #include "sr_common.cuh"
 #include "sr_internal.h"
 #include "sr_mixed_common.cuh"
+#include "sr_adjoint_common.cuh"
 
 namespace sr {
 namespace {
@@ -36,14 +37,6 @@ constexpr int kASteps = kAW * 32;     // steps per work item (one per lane)
 constexpr int kAStage = 1024;         // (direction, omega) points per constants stage
 constexpr int kARS = 8;               // omega points per phasor reseed
 constexpr int kAG = 9;                // per-step gradient components: x (3), bbar (3), a (3)
-
-struct AdjGlobals {
-  float dw_h, dw_l;        // omega spacing (rad per unit time) as a double-float
-  float w0f, dwf;          // first omega and spacing in FP32
-  float wabs_min, wabs_max;
-  int uniform;             // omega axis uniform to 1e-12
-  int pad_;
-};
 
 struct AdjParams {
   FarMixedParams f;            // tracks, grid, records, status
@@ -58,49 +51,6 @@ struct AdjParams {
   double *grad[6];             // x, y, z, ux, uy, uz  [total_steps]
   double *grad_w;              // [n_tracks]
 };
-
-// Omega table, axis uniformity and |omega| range (one block).
-__global__ void adj_globals_kernel(AdjParams a) {
-  const FarMixedParams &p = a.f;
-  const uint32_t nO = p.n_omega;
-  const double w0 = p.omega[0];
-  const double dw = (nO > 1) ? (p.omega[nO - 1] - w0) / (double)(nO - 1) : 0.0;
-  bool uni = true;
-  float amin = 3.0e38f, amax = 0.f;
-  for (uint32_t m = threadIdx.x; m < nO; m += blockDim.x) {
-    const double wm = p.omega[m];
-    if (fabs(wm - (w0 + (double)m * dw)) > 1e-12 * fabs(wm) + 1e-300) uni = false;
-    const df r = df_from_double(wm * 0.15915494309189533577);
-    const float aw = (float)fabs(wm);
-    a.wtab[m] = make_float4(r.hi, r.lo, (float)wm, aw);
-    amin = fminf(amin, aw);
-    amax = fmaxf(amax, aw);
-  }
-  __shared__ float smin[256], smax[256];
-  smin[threadIdx.x] = amin;
-  smax[threadIdx.x] = amax;
-  const int all_uni = __syncthreads_and(uni ? 1 : 0);
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if ((int)threadIdx.x < o) {
-      smin[threadIdx.x] = fminf(smin[threadIdx.x], smin[threadIdx.x + o]);
-      smax[threadIdx.x] = fmaxf(smax[threadIdx.x], smax[threadIdx.x + o]);
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    AdjGlobals g;
-    const df d = df_from_double(dw);
-    g.dw_h = d.hi;
-    g.dw_l = d.lo;
-    g.w0f = (float)w0;
-    g.dwf = (float)dw;
-    g.wabs_min = smin[0];
-    g.wabs_max = smax[0];
-    g.uniform = all_uni;
-    g.pad_ = 0;
-    *a.glob = g;
-  }
-}
 
 // 2 dt^2 g(p) in FP32, and the direction table:
 //   [0] (1 - cos theta hi, lo, n_x hi, lo)   [1] (n_y hi, lo, 1 - cos theta, n_x)
@@ -126,32 +76,6 @@ __global__ void adj_prep_kernel(AdjParams a) {
     o[2] = make_float4((float)n1, (float)cT, (float)(cT * cPh), (float)(cT * sPh));
     o[3] = make_float4((float)(-sT), (float)(-sPh), (float)cPh, 0.f);
   }
-}
-
-// Work items: ceil(n_body / 256) per track, as an exclusive prefix (one block
-// of 1024 threads, each scanning a contiguous run of tracks).
-__global__ void adj_items_kernel(AdjParams a) {
-  const FarMixedParams &p = a.f;
-  const uint32_t n = p.n_tracks;
-  const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
-  const uint32_t t0 = min(n, threadIdx.x * per), t1 = min(n, t0 + per);
-  int64_t local = 0;
-  for (uint32_t t = t0; t < t1; ++t) local += (track_body(p, t) + kASteps - 1) / kASteps;
-  __shared__ int64_t sums[1024];
-  sums[threadIdx.x] = local;
-  __syncthreads();
-  for (uint32_t off = 1; off < blockDim.x; off <<= 1) {
-    const int64_t v = threadIdx.x >= off ? sums[threadIdx.x - off] : 0;
-    __syncthreads();
-    sums[threadIdx.x] += v;
-    __syncthreads();
-  }
-  int64_t run = threadIdx.x ? sums[threadIdx.x - 1] : 0;
-  for (uint32_t t = t0; t < t1; ++t) {
-    a.item_off[t] = run;
-    run += (track_body(p, t) + kASteps - 1) / kASteps;
-  }
-  if (threadIdx.x == blockDim.x - 1) a.item_off[n] = sums[blockDim.x - 1];
 }
 
 // dL/dw_t = sum_p g(p) dt^2 |A_t(p)|^2, one block per track (fixed order).
@@ -629,13 +553,13 @@ extern "C" int sr_far_total_backward(const sr_tracks *t, const sr_grid *g,
   const int64_t step_blocks = std::max<int64_t>(
       1, std::min<int64_t>((t->total_steps + 255) / 256, (int64_t)n_sm * 128));
   if (t->total_steps > 0) launch_far_prepass(a.f, (int)step_blocks, s);
-  adj_globals_kernel<<<1, 256, 0, s>>>(a);
+  adj_globals_kernel<<<1, 256, 0, s>>>(a.f, a.wtab, a.glob);
   {
     const uint64_t work = std::max<uint64_t>(P, n_dirs);
     const uint64_t nb = std::min<uint64_t>((work + 255) / 256, (uint64_t)n_sm * 64);
     adj_prep_kernel<<<(unsigned)nb, 256, 0, s>>>(a);
   }
-  adj_items_kernel<<<1, 1024, 0, s>>>(a);
+  adj_items_kernel<<<1, 1024, 0, s>>>(a.f, a.item_off, (uint32_t)kASteps);
   adj_weight_kernel<<<t->n_tracks, 256, 0, s>>>(a);
   rc = cuda_fail(cudaGetLastError(), "adjoint prep launch");
   if (rc) return rc;

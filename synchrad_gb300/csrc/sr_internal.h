@@ -65,7 +65,9 @@ struct FarMixedParams {
   float4 *records;     // [total_steps][4]
   double *partial;     // [n_sub][n_out][n_snaps][P]
   float *outer;        // [grid][W][K][8][32] compensated per-track sums
-  float *save_A;       // optional [n_tracks][P][4]: A_theta, A_phi of each track
+  float *save_A;       // optional per-track amplitudes for the adjoints: far
+                       // [n_tracks][P][4] (A_theta, A_phi), near [n_tracks][P][8]
+                       // (A_x, A_y, A_z complex, two floats of padding)
   int *status;
   // outputs
   double *out[6];
@@ -96,6 +98,7 @@ size_t far_mixed_workspace(int64_t total_steps, uint64_t n_points, int n_out,
 int launch_far_mixed(FarMixedParams p, const FarMixedConfig &cfg,
                      void *workspace, size_t ws_bytes, cudaStream_t stream);
 void launch_far_prepass(const FarMixedParams &p, int blocks, cudaStream_t stream);
+void launch_near_prepass(const FarMixedParams &p, int blocks, cudaStream_t stream);
 
 // The mixed-precision near field (same parameter block; n_theta holds n_R,
 // sin_theta the radius axis, L_screen the screen distance).

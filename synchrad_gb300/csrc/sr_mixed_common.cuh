@@ -76,6 +76,28 @@ __device__ __noinline__ bool exact_mask(const FarMixedParams &p, int64_t base, u
   return fabs(__dsub_rn(ph, prev)) < M_PI;
 }
 
+// The reference's mask test evaluated exactly as the FP64 kernel does it
+// (synchrad/kernel_nearfield.cl:64-74), for one point and step.
+__device__ __noinline__ bool exact_mask_near(const FarMixedParams &p, int64_t base, uint32_t s,
+                                             uint32_t it_start, double omega, double P0,
+                                             double P1) {
+  auto ld = [&](const void *a, int64_t i) -> double {
+    return p.track_f32 ? (double)((const float *)a)[i] : ((const double *)a)[i];
+  };
+  auto phase_at = [&](uint32_t it) -> double {
+    const double time = __dmul_rn((double)(uint32_t)(it_start + it), p.dt);
+    const int64_t g = base + it;
+    const double d0 = __dsub_rn(P0, ld(p.x, g));
+    const double d1 = __dsub_rn(P1, ld(p.y, g));
+    const double d2 = __dsub_rn(p.L_screen, ld(p.z, g));
+    const double rr = __dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2));
+    return __dmul_rn(omega, __dadd_rn(time, __dsqrt_rn(rr)));
+  };
+  const double ph = phase_at(s);
+  const double prev = (s == 0) ? 0.0 : phase_at(s - 1);
+  return fabs(__dsub_rn(ph, prev)) < M_PI;
+}
+
 // Bits j in [0, nv) of a uniform omega chunk (omega_j = w0 + j dw) with
 // |omega_j| < wb: an index interval, found from its two float bounds.
 __device__ __forceinline__ uint32_t omega_range_bits(float w0, float dw, float wb, int nv) {

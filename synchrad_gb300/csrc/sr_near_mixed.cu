@@ -94,28 +94,6 @@ struct NearSmemFixed {
   // followed by float4 setup[W][32][dpw][kNSetupF4]
 };
 
-// The reference's mask test evaluated exactly as the FP64 kernel does it
-// (synchrad/kernel_nearfield.cl:64-74), for one point and step.
-__device__ __noinline__ bool exact_mask_near(const FarMixedParams &p, int64_t base, uint32_t s,
-                                             uint32_t it_start, double omega, double P0,
-                                             double P1) {
-  auto ld = [&](const void *a, int64_t i) -> double {
-    return p.track_f32 ? (double)((const float *)a)[i] : ((const double *)a)[i];
-  };
-  auto phase_at = [&](uint32_t it) -> double {
-    const double time = __dmul_rn((double)(uint32_t)(it_start + it), p.dt);
-    const int64_t g = base + it;
-    const double d0 = __dsub_rn(P0, ld(p.x, g));
-    const double d1 = __dsub_rn(P1, ld(p.y, g));
-    const double d2 = __dsub_rn(p.L_screen, ld(p.z, g));
-    const double rr = __dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2));
-    return __dmul_rn(omega, __dadd_rn(time, __dsqrt_rn(rr)));
-  };
-  const double ph = phase_at(s);
-  const double prev = (s == 0) ? 0.0 : phase_at(s - 1);
-  return fabs(__dsub_rn(ph, prev)) < M_PI;
-}
-
 // Packed accumulators of one lane: six complex sums for K points.
 struct NearAcc {
   float2 s1r[3][kNK / 2], s1i[3][kNK / 2];  // sum (beta - n)/r e^{i phi}, x y z
@@ -280,6 +258,11 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
             Ai[c] = val(9 + c) + w * val(c);
           }
           const uint64_t gti = (uint64_t)(j0 + m) + (uint64_t)nO * dir;
+          if (p.save_A != nullptr && ksnap == 0) {  // the adjoint's forward record
+            float4 *sa = reinterpret_cast<float4 *>(p.save_A) + 2 * ((uint64_t)t * P + gti);
+            sa[0] = make_float4((float)Ar[0], (float)Ai[0], (float)Ar[1], (float)Ai[1]);
+            sa[1] = make_float4((float)Ar[2], (float)Ai[2], 0.f, 0.f);
+          }
           auto add = [&](int c, double v) {
             part[((uint64_t)c * p.n_snaps + ksnap) * P + gti] += v;
           };
@@ -583,6 +566,14 @@ FarMixedConfig near_mixed_choose(uint32_t n_omega, uint32_t n_screen, uint32_t n
   int L = 32;
   while (L > 32 / kNMaxDpw && (uint32_t)(L / 2) * kNK >= n_omega) L /= 2;
   return near_mixed_make(n_omega, n_screen, n_tracks, n_sm, L, 0);
+}
+
+// The near-field step records for another kernel of the library (the adjoint).
+void launch_near_prepass(const FarMixedParams &p, int blocks, cudaStream_t stream) {
+  if (p.track_f32)
+    near_prepass_kernel<float><<<blocks, 256, 0, stream>>>(p);
+  else
+    near_prepass_kernel<double><<<blocks, 256, 0, stream>>>(p);
 }
 
 size_t near_mixed_workspace(int64_t total_steps, uint64_t n_points, int n_out, uint32_t n_snaps,

@@ -83,6 +83,42 @@ class Utilities:
                                        lambda0_um=lambda0_um, **kw_args)
         return _trapz(val, self.Args["omega"])
 
+    def get_energy_weights(self, lambda0_um=None):
+        """Weights q (host layout [nOmega, nTheta|nR, nPhi]) with
+        ``get_energy(lambda0_um=...) == sum(q * S)`` for a 'total' spectrum S:
+        the quadrature of get_energy_spectrum / get_energy written out, so that
+        an energy loss can be differentiated through the spectrum (no
+        counterpart in the reference)."""
+        def trapz_w(x):
+            x = np.asarray(x, dtype=np.double)
+            w = np.zeros_like(x)
+            if x.size > 1:
+                d = np.diff(x)
+                w[:-1] += 0.5 * d
+                w[1:] += 0.5 * d
+            return w
+
+        if self.Args["mode"] == "far":
+            c = alpha_fs / (4 * np.pi ** 2)
+            th = np.asarray(self.Args["theta"], dtype=np.double)
+            th_loc = 0.5 * (th[1:] + th[:-1])
+            a = trapz_w(th_loc) * np.sin(th_loc)
+            ang = np.zeros_like(th)
+            ang[:-1] += 0.5 * a
+            ang[1:] += 0.5 * a
+        elif self.Args["mode"] == "near":
+            c = alpha_fs * np.pi / 4 / (2 * np.pi) ** 2
+            r = np.asarray(self.Args["radius"], dtype=np.double)
+            ang = trapz_w(r) * r
+        else:
+            raise ValueError("energy weights are defined for the 'far' and 'near' modes")
+        if lambda0_um is not None:
+            c = c * J_in_um / lambda0_um
+        w_om = trapz_w(self.Args["omega"])
+        n_phi = len(self.Args["phi"]) if "phi" in self.Args else None
+        q = c * self.Args["dph"] * w_om[:, None] * ang[None, :]
+        return np.repeat(q[:, :, None], n_phi if n_phi else 1, axis=2)
+
     def get_spot(self, k0=None, spect_filter=None, phot_num=False, lambda0_um=None,
                  **kw_args):
         """synchrad/utils.py:104-125: angular (or screen) map, integrated over

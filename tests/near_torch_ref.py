@@ -1,0 +1,48 @@
+"""Float64 PyTorch restatement of the reference's near-field 'total' kernel
+(synchrad/kernel_nearfield.cl:58-102), differentiable by autograd.
+
+One snapshot at the end of each track (itStart = 0, itEnd = nSteps = track
+length).  The |dphase| < pi mask is computed from the phases and then held
+fixed, as the CUDA adjoint does.  Test infrastructure only.
+"""
+from __future__ import annotations
+
+import math
+
+import torch
+
+
+def near_total_torch(x, y, z, ux, uy, uz, w, offsets, dt, omega, radius, sinP, cosP, L_screen):
+    """Spectrum [nPhi, nR, nOmega] of the concatenated tracks (CSR ``offsets``)."""
+    X0 = (radius[None, :] * cosP[:, None]).reshape(-1)  # screen point index iPhi * nR + iR
+    Y0 = (radius[None, :] * sinP[:, None]).reshape(-1)
+    S = torch.zeros(X0.numel(), omega.numel(), dtype=torch.float64, device=x.device)
+    for t in range(len(offsets) - 1):
+        a0, a1 = int(offsets[t]), int(offsets[t + 1])
+        if a1 - a0 < 2:
+            continue
+        m = a1 - a0 - 1  # steps 0 .. n-2 enter the sum
+        xs, ys, zs = x[a0:a1 - 1], y[a0:a1 - 1], z[a0:a1 - 1]
+        U = torch.stack([ux[a0:a1 - 1], uy[a0:a1 - 1], uz[a0:a1 - 1]], -1)
+        B = U / torch.sqrt(1.0 + (U * U).sum(-1, keepdim=True))           # [m, 3]
+        rx = X0[None, :] - xs[:, None]
+        ry = Y0[None, :] - ys[:, None]
+        rz = (L_screen - zs)[:, None].expand_as(rx)
+        r = torch.sqrt(rx * rx + ry * ry + rz * rz)                         # [m, D]
+        n = torch.stack([rx, ry, rz], -1) / r[..., None]                   # [m, D, 3]
+        time = torch.arange(m, dtype=torch.float64, device=x.device) * dt
+        phase = omega[None, None, :] * (time[:, None, None] + r[..., None])  # [m, D, O]
+        with torch.no_grad():
+            prev = torch.cat([torch.zeros_like(phase[:1]), phase[:-1]], 0)
+            mask = (phase - prev).abs() < math.pi
+        cw = torch.where(mask, torch.cos(phase), torch.zeros_like(phase))
+        sw = torch.where(mask, torch.sin(phase), torch.zeros_like(phase))
+        c2 = n / (r * r)[..., None]                                        # [m, D, 3]
+        c1b = (B[:, None, :] - n) / r[..., None]                           # c1 / omega
+        # Re += -omega c1b sin + c2 cos;  Im += omega c1b cos + c2 sin
+        re = (torch.einsum("mdo,mdk->dok", cw, c2)
+              - omega[None, :, None] * torch.einsum("mdo,mdk->dok", sw, c1b))
+        im = (torch.einsum("mdo,mdk->dok", sw, c2)
+              + omega[None, :, None] * torch.einsum("mdo,mdk->dok", cw, c1b))
+        S = S + w[t] * dt * dt * ((re * re).sum(-1) + (im * im).sum(-1))
+    return S.reshape(sinP.numel(), radius.numel(), omega.numel())
