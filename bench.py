@@ -288,6 +288,14 @@ def adjoint_main(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
     stream = torch.cuda.current_stream(device)
     pt_steps = w.pt_steps
+    tune = None
+    if not args.no_tune:  # the forward's work shape, as for the forward benchmark
+        from synchrad_gb300.autograd import _tracks_struct
+        from synchrad_gb300.batch import autotune
+        t0 = time.perf_counter()
+        tune = autotune(_tracks_struct([c.detach() for c in coords], wt.detach(), layout),
+                        layout.grid, "total", _lib.SR_PREC_MIXED, args.tune_budget_ms, stream)
+        tune["wall_s"] = time.perf_counter() - t0
 
     def one_step(ev=None):
         flush.fill_(1.0)
@@ -366,7 +374,7 @@ def adjoint_main(args):
                            "parallelism": f"replicas x{ws} (tracks independent)"},
                 "adjoint": {"forward_ms": fwd_ms, "backward_ms": bwd_ms,
                             "backward_over_forward": bwd_ms / fwd_ms,
-                            "adjoint_kernel_ms": kern_avg},
+                            "adjoint_kernel_ms": kern_avg, "forward_autotune": tune},
                 "e2e": None, "gpu_launches": 10 * args.steps,
                 "clocks": clocks.summary(),
                 "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak,

@@ -78,27 +78,6 @@ __global__ void adj_prep_kernel(AdjParams a) {
   }
 }
 
-// dL/dw_t = sum_p g(p) dt^2 |A_t(p)|^2, one block per track (fixed order).
-__global__ void adj_weight_kernel(AdjParams a) {
-  const FarMixedParams &p = a.f;
-  const uint64_t P = (uint64_t)p.n_omega * p.n_theta * p.n_phi;
-  const uint32_t t = blockIdx.x;
-  double acc = 0.0;
-  for (uint64_t g = threadIdx.x; g < P; g += blockDim.x) {
-    const float4 A = a.save_A[(uint64_t)t * P + g];
-    const double a2 = (double)A.x * A.x + (double)A.y * A.y + (double)A.z * A.z +
-                      (double)A.w * A.w;
-    acc += a.grad_spec[g] * a2;
-  }
-  __shared__ double red[256];
-  red[threadIdx.x] = acc;
-  __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) a.grad_w[t] = red[0] * p.dt * p.dt;
-}
 
 // Per-step gradients: map dL/dbbar and dL/da of steps s-1 and s to dL/dbeta_s
 // and dL/du_s.
@@ -439,13 +418,15 @@ __global__ void __launch_bounds__(W * 32, 2) adj_far_kernel(AdjParams a) {
 size_t adj_smem_bytes() { return sizeof(AdjSmem); }
 
 struct AdjLayout {
-  size_t records, gsf, wtab, dirtab, glob, item_off, gstep, total;
+  size_t records, gsf, wtab, dirtab, glob, item_off, gstep, wpart, total;
+  uint32_t w_chunks;
 };
 
 AdjLayout adj_layout(int64_t total_steps, uint64_t P, uint32_t n_omega, uint64_t n_dirs,
                      uint32_t n_tracks) {
   auto up = [](size_t v) { return (v + 255) / 256 * 256; };
   AdjLayout l;
+  l.w_chunks = adj_weight_chunks(P, n_tracks, device_sm_count());
   l.records = 256;
   l.gsf = l.records + up((size_t)total_steps * 64);
   l.wtab = l.gsf + up((size_t)P * 4);
@@ -453,7 +434,8 @@ AdjLayout adj_layout(int64_t total_steps, uint64_t P, uint32_t n_omega, uint64_t
   l.glob = l.dirtab + up((size_t)n_dirs * 64);
   l.item_off = l.glob + 256;
   l.gstep = l.item_off + up(((size_t)n_tracks + 1) * 8);
-  l.total = l.gstep + up((size_t)total_steps * kAG * 8);
+  l.wpart = l.gstep + up((size_t)total_steps * kAG * 8);
+  l.total = l.wpart + up((size_t)n_tracks * l.w_chunks * 8);
   return l;
 }
 
@@ -560,7 +542,13 @@ extern "C" int sr_far_total_backward(const sr_tracks *t, const sr_grid *g,
     adj_prep_kernel<<<(unsigned)nb, 256, 0, s>>>(a);
   }
   adj_items_kernel<<<1, 1024, 0, s>>>(a.f, a.item_off, (uint32_t)kASteps);
-  adj_weight_kernel<<<t->n_tracks, 256, 0, s>>>(a);
+  {
+    double *wpart = (double *)(w + lay.wpart);
+    adj_weight_partial_kernel<1><<<t->n_tracks * lay.w_chunks, kWeightThreads, 0, s>>>(
+        a.save_A, grad_spectrum, P, lay.w_chunks, wpart);
+    adj_weight_final_kernel<<<(t->n_tracks + 255) / 256, 256, 0, s>>>(
+        wpart, t->n_tracks, lay.w_chunks, t->dt, grad_weight);
+  }
   rc = cuda_fail(cudaGetLastError(), "adjoint prep launch");
   if (rc) return rc;
   const size_t smem = adj_smem_bytes();

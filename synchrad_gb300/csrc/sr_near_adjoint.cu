@@ -73,29 +73,6 @@ __global__ void nadj_prep_kernel(NearAdjParams a) {
   }
 }
 
-// dL/dw_t = sum_p g(p) dt^2 |A_t(p)|^2, one block per track (fixed order).
-__global__ void nadj_weight_kernel(NearAdjParams a) {
-  const FarMixedParams &p = a.f;
-  const uint64_t P = (uint64_t)p.n_omega * p.n_theta * p.n_phi;
-  const uint32_t t = blockIdx.x;
-  double acc = 0.0;
-  for (uint64_t g = threadIdx.x; g < P; g += blockDim.x) {
-    const float4 A0 = a.save_A[2 * ((uint64_t)t * P + g)];
-    const float4 A1 = a.save_A[2 * ((uint64_t)t * P + g) + 1];
-    const double a2 = (double)A0.x * A0.x + (double)A0.y * A0.y + (double)A0.z * A0.z +
-                      (double)A0.w * A0.w + (double)A1.x * A1.x + (double)A1.y * A1.y;
-    acc += a.grad_spec[g] * a2;
-  }
-  __shared__ double red[256];
-  red[threadIdx.x] = acc;
-  __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) a.grad_w[t] = red[0] * p.dt * p.dt;
-}
-
 // dL/du_s from dL/dbeta_s (beta = u / gamma at the same step).
 template <typename TT>
 __global__ void nadj_final_kernel(NearAdjParams a) {
@@ -452,13 +429,15 @@ __global__ void __launch_bounds__(W * 32, 2) nadj_kernel(NearAdjParams a) {
 size_t nadj_smem_bytes() { return sizeof(NearAdjSmem); }
 
 struct NearAdjLayout {
-  size_t records, gsf, wtab, sctab, glob, item_off, gstep, total;
+  size_t records, gsf, wtab, sctab, glob, item_off, gstep, wpart, total;
+  uint32_t w_chunks;
 };
 
 NearAdjLayout nadj_layout(int64_t total_steps, uint64_t P, uint32_t n_omega, uint64_t n_scr,
                           uint32_t n_tracks) {
   auto up = [](size_t v) { return (v + 255) / 256 * 256; };
   NearAdjLayout l;
+  l.w_chunks = adj_weight_chunks(P, n_tracks, device_sm_count());
   l.records = 256;
   l.gsf = l.records + up((size_t)total_steps * 64);
   l.wtab = l.gsf + up((size_t)P * 4);
@@ -466,7 +445,8 @@ NearAdjLayout nadj_layout(int64_t total_steps, uint64_t P, uint32_t n_omega, uin
   l.glob = l.sctab + up((size_t)n_scr * 16);
   l.item_off = l.glob + 256;
   l.gstep = l.item_off + up(((size_t)n_tracks + 1) * 8);
-  l.total = l.gstep + up((size_t)total_steps * kNAG * 8);
+  l.wpart = l.gstep + up((size_t)total_steps * kNAG * 8);
+  l.total = l.wpart + up((size_t)n_tracks * l.w_chunks * 8);
   return l;
 }
 
@@ -573,7 +553,13 @@ extern "C" int sr_near_total_backward(const sr_tracks *t, const sr_grid *g,
     nadj_prep_kernel<<<(unsigned)nb, 256, 0, s>>>(a);
   }
   adj_items_kernel<<<1, 1024, 0, s>>>(a.f, a.item_off, (uint32_t)kNASteps);
-  nadj_weight_kernel<<<t->n_tracks, 256, 0, s>>>(a);
+  {
+    double *wpart = (double *)(w + lay.wpart);
+    adj_weight_partial_kernel<2><<<t->n_tracks * lay.w_chunks, kWeightThreads, 0, s>>>(
+        a.save_A, grad_spectrum, P, lay.w_chunks, wpart);
+    adj_weight_final_kernel<<<(t->n_tracks + 255) / 256, 256, 0, s>>>(
+        wpart, t->n_tracks, lay.w_chunks, t->dt, grad_weight);
+  }
   rc = cuda_fail(cudaGetLastError(), "near adjoint prep launch");
   if (rc) return rc;
   const size_t smem = nadj_smem_bytes();
