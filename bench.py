@@ -161,6 +161,15 @@ def make_workload(args):
 
 
 def flops_per_unit(w):
+    """Algorithmic FP32 flops per point-step (the roofline's numerator): far
+    field 18 (rotation 2 FMUL + 2 FFMA, three complex components 6 FFMA),
+    near field 30 (rotation 6, two vectors x 3 components x Re/Im 12 FFMA)."""
+    return 30 if w.args.get("mode", "far") == "near" else CANONICAL_FLOPS
+
+
+def executed_flops_per_unit(w):
+    """Flops the mixed kernels execute per point-step: the far field carries
+    A on theta-hat and phi-hat only (n.amp = 0), 2 FMUL + 6 FFMA = 14."""
     return 30 if w.args.get("mode", "far") == "near" else FLOPS_PER_UNIT
 
 
@@ -502,19 +511,22 @@ def main():
                                     ctypes.c_void_p(stream.cuda_stream)))
     kern_avg_ms = kern_ms.value / max(kern_n.value, 1)
     fpu = flops_per_unit(w)
+    fpu_exec = executed_flops_per_unit(w)
     achieved = pt_steps * fpu / (kern_avg_ms * 1e-3) / 1e12
+    achieved_exec = pt_steps * fpu_exec / (kern_avg_ms * 1e-3) / 1e12
     peak = max(tf_s.value, tf_p.value)
     clk = clocks.summary()
+    kname = "near_mixed_kernel" if mode == "near" else "far_mixed_kernel"
     roofline = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak if peak else None,
                 "traffic": None,
-                "kernel": ("near_mixed_kernel (8 omega points per lane, 8 warps per CTA)"
-                           if mode == "near" else
-                           "far_mixed_kernel (32 omega points per lane, 8 warps per CTA)"),
+                "kernel": (f"{kname} ({shape['points_per_lane']} omega points per lane, "
+                           f"{shape['lanes_per_direction']} lanes per direction, 8 warps per CTA)"),
                 "kernel_ms_avg": kern_avg_ms,
                 "flops_per_unit": fpu,
-                "frac_canonical_18_flops": (achieved * CANONICAL_FLOPS / fpu / peak
-                                            if peak and mode == "far" else None),
+                "flops_per_unit_source": "SURVEY 8(d) algorithmic work per point-step",
+                "flops_per_unit_executed": fpu_exec,
+                "frac_executed": achieved_exec / peak if peak else None,
                 "peak_source": ("measured on this GPU by sr_probe_fp32_peak (FFMA / FFMA2 "
                                 f"throughput: {tf_s.value:.1f} / {tf_p.value:.1f} TFLOP/s); "
                                 "MEASURED_PEAKS.json has no FP32 figure"),
