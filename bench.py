@@ -87,13 +87,15 @@ class ClockSampler:
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu_index: str):
+        import tempfile
         self.gpu = gpu_index
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_bench.csv"
+        fd, name = tempfile.mkstemp(prefix="sr_clocks_", suffix=".csv")
+        os.close(fd)
+        self.path = Path(name)
 
     def __enter__(self):
         try:
-            self.path.parent.mkdir(exist_ok=True)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
@@ -524,7 +526,12 @@ def main():
                            f"{shape['lanes_per_direction']} lanes per direction, 8 warps per CTA)"),
                 "kernel_ms_avg": kern_avg_ms,
                 "flops_per_unit": fpu,
-                "flops_per_unit_source": "SURVEY 8(d) algorithmic work per point-step",
+                "flops_per_unit_source": ("algorithmic work per point-step of the "
+                                          "three-component formulation (rotation 2 FMUL + "
+                                          "2 FFMA, accumulation 6 FFMA)"
+                                          if mode == "far" else
+                                          "algorithmic work per point-step (rotation 6, "
+                                          "two vectors x 3 components x Re/Im 12 FFMA)"),
                 "flops_per_unit_executed": fpu_exec,
                 "frac_executed": achieved_exec / peak if peak else None,
                 "peak_source": ("measured on this GPU by sr_probe_fp32_peak (FFMA / FFMA2 "
