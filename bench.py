@@ -594,7 +594,10 @@ def main():
             el = float(t.item())
         e2e_spec = calc.Data["radiation"]["total"]
         host_ref = mixed_spec.cpu().numpy().swapaxes(-1, -3)
-        e2e = {"value": pt_steps * ws * n_e2e / el / 1e9, "unit": UNIT,
+        # SynchRad strides the one workload over the ranks and sums on rank 0
+        # (the reference's scheme): the whole job is pt_steps per call
+        e2e = {"value": pt_steps * n_e2e / el / 1e9, "unit": UNIT,
+               "scaling": "strong" if ws > 1 else "single GPU",
                "h2d_bytes_per_step": int(batch.h2d_bytes),
                "d2h_bytes_per_step": int(P * 8),
                "steps": n_e2e, "ms_per_step": el / n_e2e * 1e3,

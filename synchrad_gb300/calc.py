@@ -348,11 +348,16 @@ class SynchRad(Utilities):
     def _gather_result_dist(self):
         """Sum the ranks' spectra and weights on rank 0 (synchrad/calc.py:560-571)."""
         dist = self.comm
+        # NCCL reduces device tensors only; gloo (and others) take host tensors
+        on_dev = (str(dist.get_backend()).lower() == "nccl" and self.device is not None)
         for key in list(self.Data["radiation"].keys()):
             t = torch.from_numpy(self.Data["radiation"][key])
+            if on_dev:
+                t = t.to(self.device)
             dist.reduce(t, dst=0)
-            self.Data["radiation"][key] = t.numpy()
-        tw = torch.tensor([float(self.total_weight)], dtype=torch.float64)
+            self.Data["radiation"][key] = t.cpu().numpy()
+        tw = torch.tensor([float(self.total_weight)], dtype=torch.float64,
+                          device=self.device if on_dev else "cpu")
         dist.reduce(tw, dst=0)
         self.total_weight = float(tw[0]) if self.rank == 0 else self.total_weight
 
