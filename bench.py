@@ -69,6 +69,10 @@ def parse():
     ap.add_argument("--tune-budget-ms", type=float, default=6000.0)
     ap.add_argument("--no-graph", action="store_true",
                     help="direct sr_spectrum calls instead of CUDA-graph replay")
+    ap.add_argument("--shape", type=int, nargs=4, default=None,
+                    metavar=("K", "L", "STAGE", "SUBSETS"),
+                    help="pin the work shape (points per lane, lanes per direction, steps per "
+                         "stage, track subsets; 0 subsets = default) instead of tuning")
     return ap.parse_args()
 
 
@@ -442,7 +446,11 @@ def main():
     stream = torch.cuda.current_stream(device)
 
     tune = None
-    if not args.no_tune:
+    if args.shape is not None:
+        from synchrad_gb300.batch import set_config
+        k_, l_, st_, ns_ = args.shape
+        set_config(batch, grid, "total", _lib.SR_PREC_MIXED, k_, l_, st_, ns_)
+    elif not args.no_tune:
         t0 = time.perf_counter()
         tune = autotune(batch, grid, "total", _lib.SR_PREC_MIXED, args.tune_budget_ms, stream)
         tune["wall_s"] = time.perf_counter() - t0
