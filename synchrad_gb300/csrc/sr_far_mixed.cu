@@ -196,6 +196,7 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
     const double w0d = nv > 0 ? p.omega[j0] : 0.0;
     const df d_w0 = df_from_double(w0d * inv2pi);
     const float w0f = (float)w0d, dwf = (float)dw_glob;
+    const float inv_dwf = (dwf != 0.f) ? 1.0f / dwf : 0.f;
     bool uniform = true;
     float wabs_min = 3.0e38f, wabs_max = 0.f;
     for (int m = 0; m < nv; ++m) {
@@ -488,8 +489,10 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
                     if (uniform) {
                       // included points form an index interval; only points
                       // inside the guard band need the exact FP64 test
-                      mask = omega_range_bits(w0f, dwf, kPiLo / adt, nv);
-                      uint32_t unc = omega_range_bits(w0f, dwf, kPiHi / adt, nv) & ~mask;
+                      const float inv_adt = __frcp_rn(adt);  // adt > 0 here
+                      mask = omega_range_bits_r(w0f, dwf, inv_dwf, kPiLo * inv_adt, nv);
+                      uint32_t unc =
+                          omega_range_bits_r(w0f, dwf, inv_dwf, kPiHi * inv_adt, nv) & ~mask;
                       while (unc) {
                         const int m = __ffs(unc) - 1;
                         unc &= unc - 1u;
@@ -537,23 +540,24 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
                         }
                       }
                     }
+                    // masked points: their phasors (not the amplitudes) are
+                    // zeroed, one packed product per chain and component
                     const int mA = 2 * q, mB = K / 2 + 2 * q;
-                    const float a0 = ((mask >> mA) & 1u) ? 1.f : 0.f;
-                    const float a1 = ((mask >> (mA + 1)) & 1u) ? 1.f : 0.f;
-                    const float b0 = ((mask >> mB) & 1u) ? 1.f : 0.f;
-                    const float b1 = ((mask >> (mB + 1)) & 1u) ? 1.f : 0.f;
-                    const float2 atA = make_float2(AT.x * a0, AT.x * a1);
-                    const float2 apA = make_float2(AT.z * a0, AT.z * a1);
-                    const float2 atB = make_float2(AT.x * b0, AT.x * b1);
-                    const float2 apB = make_float2(AT.z * b0, AT.z * b1);
-                    aTr[q] = __ffma2_rn(ZrA, atA, aTr[q]);
-                    aTi[q] = __ffma2_rn(ZiA, atA, aTi[q]);
-                    aPr[q] = __ffma2_rn(ZrA, apA, aPr[q]);
-                    aPi[q] = __ffma2_rn(ZiA, apA, aPi[q]);
-                    aTr[HP + q] = __ffma2_rn(ZrB, atB, aTr[HP + q]);
-                    aTi[HP + q] = __ffma2_rn(ZiB, atB, aTi[HP + q]);
-                    aPr[HP + q] = __ffma2_rn(ZrB, apB, aPr[HP + q]);
-                    aPi[HP + q] = __ffma2_rn(ZiB, apB, aPi[HP + q]);
+                    const float2 gA = make_float2(((mask >> mA) & 1u) ? 1.f : 0.f,
+                                                  ((mask >> (mA + 1)) & 1u) ? 1.f : 0.f);
+                    const float2 gB = make_float2(((mask >> mB) & 1u) ? 1.f : 0.f,
+                                                  ((mask >> (mB + 1)) & 1u) ? 1.f : 0.f);
+                    const float2 at = make_float2(AT.x, AT.y), ap = make_float2(AT.z, AT.w);
+                    const float2 mrA = __fmul2_rn(ZrA, gA), miA = __fmul2_rn(ZiA, gA);
+                    const float2 mrB = __fmul2_rn(ZrB, gB), miB = __fmul2_rn(ZiB, gB);
+                    aTr[q] = __ffma2_rn(mrA, at, aTr[q]);
+                    aTi[q] = __ffma2_rn(miA, at, aTi[q]);
+                    aPr[q] = __ffma2_rn(mrA, ap, aPr[q]);
+                    aPi[q] = __ffma2_rn(miA, ap, aPi[q]);
+                    aTr[HP + q] = __ffma2_rn(mrB, at, aTr[HP + q]);
+                    aTi[HP + q] = __ffma2_rn(miB, at, aTi[HP + q]);
+                    aPr[HP + q] = __ffma2_rn(mrB, ap, aPr[HP + q]);
+                    aPi[HP + q] = __ffma2_rn(miB, ap, aPi[HP + q]);
                     if (q + 1 < HP && uniform) {
                       rot2p(ZrA, ZiA, make_float2(R2.x, R2.y), make_float2(R2.z, R2.w),
                             make_float2(X.x, X.y), ZrA, ZiA);

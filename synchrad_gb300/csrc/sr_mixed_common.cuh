@@ -123,6 +123,33 @@ __device__ __forceinline__ uint32_t omega_range_bits(float w0, float dw, float w
   return upto & ~below & all;
 }
 
+// omega_range_bits with the divisions replaced by products with 1/dw and
+// with wb formed from 1/adt by the caller: the index bounds move by a few ulp
+// of (wb - w0)/dw, far inside the 4e-6 guard band between kPiLo and kPiHi.
+__device__ __forceinline__ uint32_t omega_range_bits_r(float w0, float dw, float inv_dw, float wb,
+                                                       int nv) {
+  const uint32_t all = (nv >= 32) ? 0xffffffffu : ((1u << nv) - 1u);
+  if (!(wb > 0.f)) return 0u;
+  float lo, hi;
+  if (dw > 0.f) {
+    lo = (-wb - w0) * inv_dw;
+    hi = (wb - w0) * inv_dw;
+  } else if (dw < 0.f) {
+    lo = (wb - w0) * inv_dw;
+    hi = (-wb - w0) * inv_dw;
+  } else {
+    return fabsf(w0) < wb ? all : 0u;
+  }
+  lo = fminf(fmaxf(lo, -2.f), 40.f);
+  hi = fminf(fmaxf(hi, -2.f), 40.f);
+  const int jf = max(0, (int)floorf(lo) + 1);      // first j > lo
+  const int jl = min(nv - 1, (int)ceilf(hi) - 1);  // last j < hi
+  if (jf > jl) return 0u;
+  const uint32_t upto = (jl >= 31) ? 0xffffffffu : ((2u << jl) - 1u);
+  const uint32_t below = (1u << jf) - 1u;
+  return upto & ~below & all;
+}
+
 // (zr + i zi) * (rc + i rs) for two points at once, factors given as pairs.
 __device__ __forceinline__ void rot2p(float2 zr, float2 zi, float2 rc, float2 rs, float2 nrs,
                                       float2 &or_, float2 &oi) {
