@@ -99,33 +99,10 @@ __device__ __noinline__ bool exact_mask_near(const FarMixedParams &p, int64_t ba
 }
 
 // Bits j in [0, nv) of a uniform omega chunk (omega_j = w0 + j dw) with
-// |omega_j| < wb: an index interval, found from its two float bounds.
-__device__ __forceinline__ uint32_t omega_range_bits(float w0, float dw, float wb, int nv) {
-  const uint32_t all = (nv >= 32) ? 0xffffffffu : ((1u << nv) - 1u);
-  if (!(wb > 0.f)) return 0u;
-  float lo, hi;
-  if (dw > 0.f) {
-    lo = (-wb - w0) / dw;
-    hi = (wb - w0) / dw;
-  } else if (dw < 0.f) {
-    lo = (wb - w0) / dw;
-    hi = (-wb - w0) / dw;
-  } else {
-    return fabsf(w0) < wb ? all : 0u;
-  }
-  lo = fminf(fmaxf(lo, -2.f), 40.f);
-  hi = fminf(fmaxf(hi, -2.f), 40.f);
-  const int jf = max(0, (int)floorf(lo) + 1);  // first j > lo
-  const int jl = min(nv - 1, (int)ceilf(hi) - 1);  // last j < hi
-  if (jf > jl) return 0u;
-  const uint32_t upto = (jl >= 31) ? 0xffffffffu : ((2u << jl) - 1u);
-  const uint32_t below = (1u << jf) - 1u;
-  return upto & ~below & all;
-}
-
-// omega_range_bits with the divisions replaced by products with 1/dw and
-// with wb formed from 1/adt by the caller: the index bounds move by a few ulp
-// of (wb - w0)/dw, far inside the 4e-6 guard band between kPiLo and kPiHi.
+// |omega_j| < wb: an index interval, found from its two float bounds.  The
+// caller passes 1/dw and forms wb from 1/adt: products instead of divisions
+// move the bounds by a few ulp of (wb - w0)/dw, far inside the 4e-6 guard
+// band between kPiLo and kPiHi.
 __device__ __forceinline__ uint32_t omega_range_bits_r(float w0, float dw, float inv_dw, float wb,
                                                        int nv) {
   const uint32_t all = (nv >= 32) ? 0xffffffffu : ((1u << nv) - 1u);

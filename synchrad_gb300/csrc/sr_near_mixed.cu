@@ -434,8 +434,11 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
                     if (uniform) {
                       // included points form an index interval; only points
                       // inside the guard band need the exact FP64 test
-                      mask = omega_range_bits(w0f, dwf, kPiLo / adt, nv);
-                      uint32_t unc = omega_range_bits(w0f, dwf, kPiHi / adt, nv) & ~mask;
+                      const float inv_adt = __frcp_rn(adt);  // adt > 0 here
+                      const float inv_dwf = (dwf != 0.f) ? __frcp_rn(dwf) : 0.f;
+                      mask = omega_range_bits_r(w0f, dwf, inv_dwf, kPiLo * inv_adt, nv);
+                      uint32_t unc =
+                          omega_range_bits_r(w0f, dwf, inv_dwf, kPiHi * inv_adt, nv) & ~mask;
                       while (unc) {
                         const int m = __ffs(unc) - 1;
                         unc &= unc - 1u;
