@@ -260,6 +260,14 @@ int sr_timing_read(double *total_ms, int *n_launches);
  * per FMA) with scalar FFMA and with packed FFMA2 instructions. */
 int sr_probe_fp32_peak(double *tflops_scalar, double *tflops_packed, void *stream);
 
+/* Failure-path self-test: launches a one-warp kernel whose bounded wait (the
+ * mbarrier wait every kernel of the library uses) is on a barrier nothing
+ * completes, with a limit of limit_ns (1 .. 1e9); the kernel records the
+ * timeout in the status word at the start of `workspace` (>= 4 bytes) as the
+ * spectrum kernels do, and sr_workspace_status then returns SR_ERR_TIMEOUT.
+ * No copy is issued and the context stays usable. */
+int sr_selftest_wait_timeout(int64_t limit_ns, void *workspace, void *stream);
+
 /* ---------------------------------------------------------------------------
  * Per-track entry points: the reference's OpenCL kernels, one launch each.
  *

@@ -111,6 +111,7 @@ EXPORTS = (
     "sr_autotune", "sr_config_get", "sr_config_set", "sr_config_clear", "sr_graph_create", "sr_graph_launch",
     "sr_graph_nodes", "sr_graph_destroy", "sr_near_total_forward_saved",
     "sr_near_total_backward_workspace_bytes", "sr_near_total_backward",
+    "sr_selftest_wait_timeout",
 )
 
 _lock = threading.Lock()
@@ -166,6 +167,8 @@ def _declare(L: ctypes.CDLL) -> None:
         bw.restype = i32
         bw.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid), vp, vp,
                        ctypes.POINTER(vp), vp, vp, ctypes.c_size_t, vp]
+    L.sr_selftest_wait_timeout.restype = i32
+    L.sr_selftest_wait_timeout.argtypes = [ctypes.c_int64, vp, vp]
     L.sr_workspace_bytes.restype = ctypes.c_int64
     L.sr_workspace_bytes.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid), i32, i32]
     L.sr_workspace_status.restype = i32

@@ -149,3 +149,36 @@ extern "C" int sr_probe_fp32_peak(double *tflops_scalar, double *tflops_packed, 
   if (tflops_packed) *tflops_packed = res[1];
   return SR_OK;
 }
+
+namespace sr {
+namespace {
+
+// A wait that nothing ends: an mbarrier expecting one arrival that never
+// comes, waited on with the bounded wait every kernel of the library uses.
+// The wait gives up after limit_ns and the kernel records the timeout in the
+// status word exactly as the spectrum kernels do; no copy is ever issued.
+__global__ void wait_timeout_selftest_kernel(int *status, uint64_t limit_ns) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const bool ok = mbar_wait_bounded(&bar, 0u, limit_ns);
+  if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicExch(status, STATUS_WAIT_TIMEOUT);
+}
+
+}  // namespace
+}  // namespace sr
+
+extern "C" int sr_selftest_wait_timeout(int64_t limit_ns, void *workspace, void *stream) {
+  clear_error();
+  if (!workspace) return fail(SR_ERR_INVALID, "workspace is NULL");
+  if (limit_ns <= 0 || limit_ns > 1000000000ll)
+    return fail(SR_ERR_INVALID, "limit %lld ns (1 .. 1e9)", (long long)limit_ns);
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaMemsetAsync(workspace, 0, sizeof(int), s);
+  if (e != cudaSuccess) return cuda_fail(e, "status reset");
+  wait_timeout_selftest_kernel<<<1, 32, 0, s>>>((int *)workspace, (uint64_t)limit_ns);
+  return cuda_fail(cudaGetLastError(), "self-test launch");
+}
