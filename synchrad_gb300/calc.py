@@ -17,6 +17,8 @@ Differences from the reference, all deliberate:
     summed on rank 0, as ``synchrad/calc.py:212, 236, 560-571`` do;
   * tracks whose ``itEnd`` or step count is 0 are rejected with ValueError (the
     reference's unsigned loop bounds wrap around for them).
+Addition: ``Args['autotune']`` (True, or a budget in ms) tunes the work shape
+of the 'mixed' kernels once per batch size before its first evaluation.
 """
 from __future__ import annotations
 
@@ -24,7 +26,8 @@ import numpy as np
 import torch
 
 from . import _lib
-from .batch import Workspace, make_grid, pack_tracks, precision_id, run_spectrum, snap_iterations
+from .batch import (Workspace, autotune, make_grid, pack_tracks, precision_id, run_spectrum,
+                    snap_iterations)
 from .utils import Utilities
 
 VEC_COMPS = {
@@ -149,8 +152,16 @@ class SynchRad(Utilities):
             last = int(np.asarray(tracks[-1][0]).size)
             self.snap_iterations = snap_iterations((0, last), nSnaps)
         outs = [self._spect_dev[k] for k in VEC_COMPS[comp]]
-        run_spectrum(batch, self._grid_dev, comp,
-                     precision_id(name, "native" in self.Args), outs,
+        prec = precision_id(name, "native" in self.Args)
+        tune = self.Args.get("autotune")  # not a reference key: True or a budget in ms
+        if tune and name == "mixed":
+            key = (batch.n_tracks, batch.total_steps, comp, int(nSnaps))
+            done = self.__dict__.setdefault("_tuned", set())
+            if key not in done:
+                budget = 3000.0 if tune is True else float(tune)
+                autotune(batch, self._grid_dev, comp, prec, budget)
+                done.add(key)
+        run_spectrum(batch, self._grid_dev, comp, prec, outs,
                      workspace=self._workspace, check_status=True)
 
     def _read_tracks(self, file_tracks, it_range, nSnaps, Np_max, verbose):

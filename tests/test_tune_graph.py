@@ -130,3 +130,22 @@ def test_config_set_rejects_bad_shapes():
         args.update(kw)
         with pytest.raises(_lib.SynchRadError):
             bt.set_config(batch, grid, **args)
+
+
+def test_synchrad_autotune_arg():
+    """Args['autotune'] tunes once per batch size inside calculate_spectrum."""
+    _need_gpu()
+    from synchrad_gb300 import _lib
+    from synchrad_gb300.calc import SynchRad
+    _lib.lib().sr_config_clear()
+    w = wl.c2_far_mixed(n_tracks=8, n_steps=400, grid=(64, 8, 8))
+    tuned = SynchRad({"grid": w.args["grid"], "dtype": "mixed", "autotune": 300})
+    tuned.calculate_spectrum([list(t) for t in w.tracks], timeStep=w.time_step, verbose=False)
+    assert len(tuned._tuned) == 1
+    tuned.calculate_spectrum([list(t) for t in w.tracks], timeStep=w.time_step, verbose=False)
+    assert len(tuned._tuned) == 1  # the second call reuses the tuned shape
+    ref = SynchRad({"grid": w.args["grid"], "dtype": "double"})
+    ref.calculate_spectrum([list(t) for t in w.tracks], timeStep=w.time_step, verbose=False)
+    got, exp = tuned.Data["radiation"]["total"], ref.Data["radiation"]["total"]
+    assert _rel(got, exp) <= TOL_MIXED
+    _lib.lib().sr_config_clear()
