@@ -9,7 +9,7 @@ parity tests can replay them without regenerating anything.
 
 Run from the repository root, where the reference tree is available:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [name-prefix ...]
 """
 from __future__ import annotations
 
@@ -108,12 +108,28 @@ def cases():
     yield ("far_total_snaps_stuck", {"grid": far_grid, "dtype": "double"}, short,
            dict(timeStep=dts, comp="total", nSnaps=9))
 
+    # the near field through the same host rules: it_range with per-track
+    # it_start and 4 snapshots, ragged tracks with mean-normalised weights, a
+    # log-spaced omega axis, repeated snapshot iterations
+    near_args = {"grid": near_grid, "mode": "near", "dtype": "double"}
+    yield ("near_total_itrange", near_args, t3,
+           dict(timeStep=dt3, comp="total", nSnaps=4, it_range=(0, 90), L_screen=1000.0))
+    yield ("near_total_ragged_wmean", near_args, rag,
+           dict(timeStep=dt, comp="total", nSnaps=2, weights_normalize="mean", L_screen=1000.0))
+    yield ("near_total_logGrid", dict(near_args, Features=["logGrid"]), tr,
+           dict(timeStep=dt, comp="total", nSnaps=1, L_screen=1000.0))
+    yield ("near_cartesian_snaps_repeat", near_args, short,
+           dict(timeStep=dts, comp="cartesian", nSnaps=8, it_range=(2, 8), L_screen=1000.0))
 
-def main():
+
+def main(only=()):
+    """Write every case, or only those whose names start with one of `only`."""
     if not oracle.ref_available():
         raise SystemExit("oracle/_ref is not buildable here (reference tree missing)")
     manifest = {}
     for name, args, tracks, kw in cases():
+        if only and not any(name.startswith(o) for o in only):
+            continue
         call = dict(kw)
         rad, tw, snaps, a = host.calculate_spectrum(
             args, [list(t) for t in tracks], kind="ref", nthreads=4, **call)
@@ -125,6 +141,10 @@ def main():
                 [float(t[6]), float(t[7]) if len(t) == 8 else -1.0])
         for key, arr in rad.items():
             data[f"out_{key}"] = arr
+        # the omega axis the reference was evaluated on: a log-spaced axis
+        # comes from np.exp, whose last bit depends on the platform, and a
+        # near-field phase of ~1e8 rad turns one ulp of omega into ~1e-8 rad
+        data["omega"] = np.asarray(a["omega"])
         data["total_weight"] = np.array(float(tw))
         data["snap_iterations"] = np.asarray(snaps)
         meta = {"args": {k: (list(map(list, v[:-1])) + [list(v[-1])] if k == "grid" else v)
@@ -138,4 +158,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

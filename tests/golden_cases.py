@@ -20,6 +20,7 @@ class GoldenCase:
     expected: dict
     total_weight: float
     snap_iterations: np.ndarray
+    omega: np.ndarray | None = None   # the axis the expected values were computed on
 
     def fresh_tracks(self):
         """Deep copies in the reference list format (the call may mutate weights)."""
@@ -56,4 +57,5 @@ def load(name: str) -> GoldenCase:
         call["it_range"] = tuple(call["it_range"])
     expected = {k[4:]: d[k] for k in d.files if k.startswith("out_")}
     return GoldenCase(name, meta["args"], call, tracks, expected,
-                      float(d["total_weight"]), d["snap_iterations"])
+                      float(d["total_weight"]), d["snap_iterations"],
+                      d["omega"] if "omega" in d.files else None)
