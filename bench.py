@@ -633,7 +633,8 @@ def main():
                            "comp": "total", "pt_steps_per_step": pt_steps,
                            "l2": "flushed before every timed step (256 MB write, counted); "
                                  f"step records ({batch.total_steps * 64 / 1e6:.0f} MB) "
-                                 "exceed L2",
+                                 + ("exceed L2" if batch.total_steps * 64 > 129e6
+                                    else "fit in L2"),
                            "parallelism": f"replicas x{ws} (tracks independent)"},
                 "e2e": e2e, "gpu_launches": 3 * args.steps,
                 "launch": {"cuda_graph": graph is not None,

@@ -91,7 +91,7 @@ struct NearSmemFixed {
   uint64_t bar[2];
   uint64_t pad_[2];
   ScreenConst sc[W][kNMaxDpw];
-  // followed by float4 setup[W][32][dpw][kNSetupF4]
+  // followed by float4 setup[W][dpw][kNSetupF4][32]
 };
 
 // Packed accumulators of one lane: six complex sums for K points.
@@ -284,12 +284,19 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
         }
       };
 
-      // One fully included step on a uniform axis: two packed chains of pairs.
-      auto step_fast = [&](const float4 *st) {
-        const float4 A = st[0], F1 = st[1], F2 = st[2], F3 = st[3], R2 = st[4], X = st[5],
-                     Y = st[6];
+      // The first pair's phasors of one step: the reseed e^{i omega_0 tau} and
+      // its product with R = e^{i d_omega tau}.
+      auto step_seed = [&](const float4 *st, float2 &ZrA, float2 &ZiA) {
+        const float4 A = st[0];
         float zs, zc;
         phasor_rev(d_w0.hi, d_w0.lo, A.x, A.y, zs, zc);
+        ZrA = make_float2(zc, zc * A.z - zs * A.w);
+        ZiA = make_float2(zs, zc * A.w + zs * A.z);
+      };
+      // One fully included step on a uniform axis: two packed chains of pairs.
+      auto step_fast = [&](const float4 *st, float2 ZrA, float2 ZiA) {
+        const float4 F1 = st[1 * 32], F2 = st[2 * 32], F3 = st[3 * 32], R2 = st[4 * 32],
+                     X = st[5 * 32], Y = st[6 * 32];
         const float2 aa[3] = {make_float2(F1.x, F1.y), make_float2(F1.z, F1.w),
                               make_float2(F2.x, F2.y)};
         const float2 bb[3] = {make_float2(F2.z, F2.w), make_float2(F3.x, F3.y),
@@ -297,8 +304,6 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
         const float2 r2c = make_float2(R2.x, R2.y), r2s = make_float2(R2.z, R2.w);
         const float2 nr2s = make_float2(X.x, X.y), hc = make_float2(X.z, X.w);
         const float2 hs = make_float2(Y.x, Y.y), nhs = make_float2(Y.z, Y.w);
-        float2 ZrA = make_float2(zc, zc * A.z - zs * A.w);
-        float2 ZiA = make_float2(zs, zc * A.w + zs * A.z);
         float2 ZrB, ZiB;
         rot2p(ZrA, ZiA, hc, hs, nhs, ZrB, ZiB);
 #pragma unroll
@@ -387,15 +392,16 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
                 cmul(Rc, Rs, Rc, Rs, R2c, R2s);
                 float Hc, Hs;
                 cmul(R2c, R2s, R2c, R2s, Hc, Hs);  // R^4 = R^(K/2)
-                float4 *st = setup + ((size_t)lane * dpw + dd) * kNSetupF4;
-                st[0] = make_float4(tau.hi, tau.lo, Rc, Rs);
-                st[1] = make_float4(ax, ax, ay, ay);
-                st[2] = make_float4(az, az, bx, bx);
-                st[3] = make_float4(by, by, bz, bz);
-                st[4] = make_float4(R2c, R2c, R2s, R2s);
-                st[5] = make_float4(-R2s, -R2s, Hc, Hc);
-                st[6] = make_float4(Hs, Hs, -Hs, -Hs);
-                st[7] = make_float4(fabsf(dtau), 0.f, 0.f, 0.f);
+                // setup[dd][k][step]: consecutive lanes store consecutive float4
+                float4 *st = setup + (size_t)dd * kNSetupF4 * 32 + lane;
+                st[0 * 32] = make_float4(tau.hi, tau.lo, Rc, Rs);
+                st[1 * 32] = make_float4(ax, ax, ay, ay);
+                st[2 * 32] = make_float4(az, az, bx, bx);
+                st[3 * 32] = make_float4(by, by, bz, bz);
+                st[4 * 32] = make_float4(R2c, R2c, R2s, R2s);
+                st[5 * 32] = make_float4(-R2s, -R2s, Hc, Hc);
+                st[6 * 32] = make_float4(Hs, Hs, -Hs, -Hs);
+                st[7 * 32] = make_float4(fabsf(dtau), 0.f, 0.f, 0.f);
                 const float am = (uint32_t)lane < mcnt ? fabsf(dtau) : 0.f;
                 const float amax =
                     __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(am)));
@@ -412,22 +418,30 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
             // general one (lanes of a warp never diverge between the two)
             if (__all_sync(0xffffffffu, uniform && !fire_here &&
                            wabs_max * sm.sc[warp][dsub].adt_max < kPiLo)) {
-              const float4 *st = setup + (size_t)dsub * kNSetupF4;
-              const size_t stride = (size_t)dpw * kNSetupF4;
-              for (uint32_t i = 0; i < mcnt; ++i, st += stride) step_fast(st);
+              // the next step's reseed is issued before this step's sums
+              const float4 *st = setup + (size_t)dsub * kNSetupF4 * 32;
+              float2 zr, zi;
+              step_seed(st, zr, zi);
+              for (uint32_t i = 0; i < mcnt; ++i) {
+                float2 zr_n, zi_n;
+                step_seed(st + min(i + 1, mcnt - 1), zr_n, zi_n);
+                step_fast(st + i, zr, zi);
+                zr = zr_n;
+                zi = zi_n;
+              }
             } else {
 #pragma unroll 1
               for (uint32_t i = 0; i < mcnt; ++i) {
-                const float4 *st = setup + ((size_t)i * dpw + dsub) * kNSetupF4;
-                const float adt = st[7].x;
+                const float4 *st = setup + (size_t)dsub * kNSetupF4 * 32 + i;
+                const float adt = st[7 * 32].x;
                 const uint32_t s = s0 + c0 + i;
                 const bool all_in = wabs_max * adt < kPiLo;
                 const bool all_out = wabs_min * adt > kPiHi;
                 // one masked path for every lane of the warp (excluded lanes
                 // carry a zero mask); skipped only when the whole warp is out
                 if (!__all_sync(0xffffffffu, all_out || nv == 0)) {
-                  const float4 A = st[0], F1 = st[1], F2 = st[2], F3 = st[3], R2 = st[4],
-                               X = st[5], Y = st[6];
+                  const float4 A = st[0], F1 = st[1 * 32], F2 = st[2 * 32], F3 = st[3 * 32],
+                               R2 = st[4 * 32], X = st[5 * 32], Y = st[6 * 32];
                   uint32_t mask = (all_out || nv == 0) ? 0u : 0xffffffffu;
                   if (!all_in && !all_out && nv > 0) {
                     const ScreenConst &c = sm.sc[warp][dsub];

@@ -117,6 +117,34 @@ def test_far_stage_sizes_agree(stage):
     assert _rel(got, ref) <= TOL_MIXED
 
 
+@pytest.mark.parametrize("L", [8, 16, 32])
+@pytest.mark.parametrize("case", ["included", "masked"])
+def test_near_shapes_agree(L, case):
+    """The near-field kernel at every lane count stays within the mixed
+    tolerance of the FP64 kernel, on an omega axis that is no multiple of the
+    lane tile; "masked" starts the axis at 0 on coarse tracks so the
+    |dphase| < pi mask cuts through it."""
+    K = 8
+    _need_gpu()
+    from synchrad_gb300 import _lib
+    from synchrad_gb300 import batch as bt
+    w = wl.c5_near_helical(n_tracks=6, n_steps=800 if case == "included" else 150,
+                           grid=(70, 6, 5))
+    if case == "masked":
+        g = list(w.args["grid"])
+        g[0] = (0.0, g[0][1])
+        w.args["grid"] = g
+    batch, grid, n = _setup(w)
+    ref = _spectrum(batch, grid, n, _lib.SR_PREC_DOUBLE)
+    _lib.lib().sr_config_clear()
+    bt.set_config(batch, grid, points_per_lane=K, lanes_per_direction=L, steps_per_stage=128)
+    used = bt.current_config(batch, grid)
+    assert used["points_per_lane"] == K and used["lanes_per_direction"] == L
+    got = _spectrum(batch, grid, n, _lib.SR_PREC_MIXED)
+    _lib.lib().sr_config_clear()
+    assert _rel(got, ref) <= TOL_MIXED
+
+
 def test_config_set_rejects_bad_shapes():
     _need_gpu()
     import ctypes
