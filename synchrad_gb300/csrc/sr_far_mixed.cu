@@ -121,7 +121,7 @@ struct SmemFixed {
   uint64_t bar[2];
   uint64_t pad_[2];
   DirConst dc[W][kMaxDpw];
-  // followed by float4 setup[W][32][dpw][6], then the two stage buffers of
+  // followed by float4 setup[W][dpw][6][32], then the two stage buffers of
   // p.stage_steps step records each
 };
 
@@ -411,13 +411,14 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
                   if (e & 1) cmul(Hc, Hs, Pc, Ps, Hc, Hs);
                   cmul(Pc, Ps, Pc, Ps, Pc, Ps);
                 }
-                float4 *st = setup + ((size_t)lane * dpw + dd) * 6;
-                st[0] = make_float4(tau.hi, tau.lo, Rc, Rs);
-                st[1] = make_float4(amp_t, amp_t, amp_p, amp_p);
-                st[2] = make_float4(R2c, R2c, R2s, R2s);
-                st[3] = make_float4(-R2s, -R2s, Hc, Hc);
-                st[4] = make_float4(Hs, Hs, -Hs, -Hs);
-                st[5] = make_float4(fabsf(dtau), 0.f, 0.f, 0.f);
+                // setup[dd][k][step]: consecutive lanes store consecutive float4
+                float4 *st = setup + (size_t)dd * 6 * 32 + lane;
+                st[0 * 32] = make_float4(tau.hi, tau.lo, Rc, Rs);
+                st[1 * 32] = make_float4(amp_t, amp_t, amp_p, amp_p);
+                st[2 * 32] = make_float4(R2c, R2c, R2s, R2s);
+                st[3 * 32] = make_float4(-R2s, -R2s, Hc, Hc);
+                st[4 * 32] = make_float4(Hs, Hs, -Hs, -Hs);
+                st[5 * 32] = make_float4(fabsf(dtau), 0.f, 0.f, 0.f);
                 // largest |dtau| of the chunk: decides the chunk's fast loop
                 const float am = (uint32_t)lane < mcnt ? fabsf(dtau) : 0.f;
                 const float amax = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(am)));
@@ -433,17 +434,22 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
             // with a uniform axis and no snapshot write, runs the tight loop.
             const bool fire_here = snap.fire_it >= (int64_t)(s0 + c0) &&
                                    snap.fire_it < (int64_t)(s0 + c0 + mcnt);
-            // One fully included step on a uniform axis: two packed chains.
-            auto step_fast = [&](const float4 *st) {
-              const float4 A = st[0], AT = st[1], R2 = st[2], X = st[3], Y = st[4];
+            // The first pair's phasors of one step: the reseed e^{i omega_0 tau}
+            // and its product with R = e^{i d_omega tau}.
+            auto step_seed = [&](const float4 *st, float2 &ZrA, float2 &ZiA) {
+              const float4 A = st[0];
               float zs, zc;
               phasor_rev(d_w0.hi, d_w0.lo, A.x, A.y, zs, zc);
+              ZrA = make_float2(zc, zc * A.z - zs * A.w);
+              ZiA = make_float2(zs, zc * A.w + zs * A.z);
+            };
+            // One fully included step on a uniform axis: two packed chains.
+            auto step_fast = [&](const float4 *st, float2 ZrA, float2 ZiA) {
+              const float4 AT = st[1 * 32], R2 = st[2 * 32], X = st[3 * 32], Y = st[4 * 32];
               const float2 at = make_float2(AT.x, AT.y), ap = make_float2(AT.z, AT.w);
               const float2 r2c = make_float2(R2.x, R2.y), r2s = make_float2(R2.z, R2.w);
               const float2 nr2s = make_float2(X.x, X.y), hc = make_float2(X.z, X.w);
               const float2 hs = make_float2(Y.x, Y.y), nhs = make_float2(Y.z, Y.w);
-              float2 ZrA = make_float2(zc, zc * A.z - zs * A.w);
-              float2 ZiA = make_float2(zs, zc * A.w + zs * A.z);
               float2 ZrB, ZiB;
               rot2p(ZrA, ZiA, hc, hs, nhs, ZrB, ZiB);
 #pragma unroll
@@ -466,23 +472,27 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
             // general one (lanes of a warp never diverge between the two)
             if (__all_sync(0xffffffffu, uniform && !fire_here &&
                            wabs_max * sm.dc[warp][dsub].adt_max < kPiLo)) {
-              const float4 *st = setup + (size_t)dsub * 6;
-              const size_t stride = (size_t)dpw * 6;
-              for (uint32_t i = 0; i < mcnt; ++i, st += stride) step_fast(st);
+              const float4 *st = setup + (size_t)dsub * 6 * 32;
+              for (uint32_t i = 0; i < mcnt; ++i) {
+                float2 zr, zi;
+                step_seed(st + i, zr, zi);
+                step_fast(st + i, zr, zi);
+              }
             } else {
               // General loop: per-step decision, per-point mask where the
               // phase advance straddles pi, non-uniform omega, snapshot writes.
 #pragma unroll 1
               for (uint32_t i = 0; i < mcnt; ++i) {
-                const float4 *st = setup + ((size_t)i * dpw + dsub) * 6;
-                const float adt = st[5].x;
+                const float4 *st = setup + (size_t)dsub * 6 * 32 + i;
+                const float adt = st[5 * 32].x;
                 const uint32_t s = s0 + c0 + i;
                 const bool all_in = wabs_max * adt < kPiLo;
                 const bool all_out = wabs_min * adt > kPiHi;
                 // one masked path for every lane of the warp (excluded lanes
                 // carry a zero mask); skipped only when the whole warp is out
                 if (!__all_sync(0xffffffffu, all_out || nv == 0)) {
-                  const float4 A = st[0], AT = st[1], R2 = st[2], X = st[3], Y = st[4];
+                  const float4 A = st[0], AT = st[1 * 32], R2 = st[2 * 32], X = st[3 * 32],
+                               Y = st[4 * 32];
                   uint32_t mask = (all_out || nv == 0) ? 0u : 0xffffffffu;
                   if (!all_in && !all_out && nv > 0) {
                     const DirConst &d = sm.dc[warp][dsub];

@@ -418,16 +418,11 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
             // general one (lanes of a warp never diverge between the two)
             if (__all_sync(0xffffffffu, uniform && !fire_here &&
                            wabs_max * sm.sc[warp][dsub].adt_max < kPiLo)) {
-              // the next step's reseed is issued before this step's sums
               const float4 *st = setup + (size_t)dsub * kNSetupF4 * 32;
-              float2 zr, zi;
-              step_seed(st, zr, zi);
               for (uint32_t i = 0; i < mcnt; ++i) {
-                float2 zr_n, zi_n;
-                step_seed(st + min(i + 1, mcnt - 1), zr_n, zi_n);
+                float2 zr, zi;
+                step_seed(st + i, zr, zi);
                 step_fast(st + i, zr, zi);
-                zr = zr_n;
-                zi = zi_n;
               }
             } else {
 #pragma unroll 1
