@@ -122,7 +122,7 @@ int sr_spectrum(const sr_tracks *tracks, const sr_grid *grid, int comp,
  * memory themselves (code embedded in a host application that owns every
  * allocation and hands over only input and output buffers): the scratch lives
  * in a 64 MiB array compiled into this library, held by every GPU that loads
- * it until the process exits.  Sizes whose scratch (64 B per track step, 8 B
+ * it until the process exits.  Sizes whose scratch (80 B per track step, 8 B
  * per point x output x snapshot, plus per-CTA sums) exceeds it are rejected
  * with SR_ERR_INVALID.  The first call on a device looks up the array's device
  * address (make it before any stream capture); calls that overlap on the GPU

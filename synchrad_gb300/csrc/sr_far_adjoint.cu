@@ -123,8 +123,7 @@ __global__ void adj_final_kernel(AdjParams a) {
 //   [0] (U_th re m, m+1, -Im U_th m, m+1)   [1] the same for U_ph
 //   [2] (Re W_th m, m+1, Im W_th m, m+1)    [3] the same for W_ph
 //   [4] (omega/2pi hi, lo of m, of m+1)     [5] (|omega| of m, m+1, 0, 0)
-constexpr int kARecS = kRecF4 + 1;  // record stride in shared memory (80 bytes: the
-                                    // per-lane record reads are free of bank conflicts)
+constexpr int kARecS = kRecF4;  // record stride in shared memory (80 bytes, as in HBM)
 
 struct AdjSmem {
   float4 rec[kASteps + 1][kARecS];  // step records r0 - 1 .. r0 + 255
@@ -198,15 +197,11 @@ __global__ void __launch_bounds__(W * 32, 2) adj_far_kernel(AdjParams a) {
     const uint32_t r1 = min(n_body, r0 + kASteps);
     const uint32_t has_prev = r0 > 0 ? 1u : 0u;
     const uint32_t n_rec = r1 - r0 + has_prev;
-    if (warp == 0) {  // one 64-byte bulk copy per record, spread over the lanes
-      if (lane == 0) {
-        fence_proxy_async();
-        mbar_arrive_expect_tx(&sm.bar, n_rec * 64u);
-      }
-      __syncwarp();
-      const float4 *src = p.records + (base + r0 - has_prev) * kRecF4;
-      for (uint32_t i = lane; i < n_rec; i += 32)
-        bulk_g2s(sm.rec[i], src + (uint64_t)i * kRecF4, 64u, &sm.bar);
+    if (threadIdx.x == 0) {  // the item's records in one bulk copy
+      fence_proxy_async();
+      mbar_arrive_expect_tx(&sm.bar, n_rec * kRecBytes);
+      bulk_g2s(sm.rec[0], p.records + (base + r0 - has_prev) * kRecF4, n_rec * kRecBytes,
+               &sm.bar);
     }
     const bool ok = mbar_wait_bounded(&sm.bar, it_no & 1u, kWaitLimitNs);
     if (__syncthreads_or(!ok)) {
@@ -428,7 +423,7 @@ AdjLayout adj_layout(int64_t total_steps, uint64_t P, uint32_t n_omega, uint64_t
   AdjLayout l;
   l.w_chunks = adj_weight_chunks(P, n_tracks, device_sm_count());
   l.records = 256;
-  l.gsf = l.records + up((size_t)total_steps * 64);
+  l.gsf = l.records + up((size_t)total_steps * kRecBytes);
   l.wtab = l.gsf + up((size_t)P * 4);
   l.dirtab = l.wtab + up((size_t)n_omega * 16);
   l.glob = l.dirtab + up((size_t)n_dirs * 64);

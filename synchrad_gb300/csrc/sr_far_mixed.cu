@@ -76,7 +76,7 @@ __global__ void far_prepass_kernel(FarMixedParams p) {
     float4 *rec = p.records + g * kRecF4;
     if (s + 1 >= n) {
       const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-      rec[0] = zero; rec[1] = zero; rec[2] = zero; rec[3] = zero;
+      rec[0] = zero; rec[1] = zero; rec[2] = zero; rec[3] = zero; rec[4] = zero;
       continue;
     }
     const double time = (double)(uint32_t)(p.it_start[t] + (uint32_t)s) * p.dt;
@@ -220,8 +220,9 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
       const uint32_t cnt = min(S, track_body(p, cur_t));
       const int b = stage_no & 1;
       fence_proxy_async();
-      mbar_arrive_expect_tx(&sm.bar[b], cnt * 64u);
-      bulk_g2s(stage_buf[b], p.records + (p.offsets[cur_t]) * kRecF4, cnt * 64u, &sm.bar[b]);
+      mbar_arrive_expect_tx(&sm.bar[b], cnt * kRecBytes);
+      bulk_g2s(stage_buf[b], p.records + (p.offsets[cur_t]) * kRecF4, cnt * kRecBytes,
+               &sm.bar[b]);
     }
 
     for (uint32_t t = t0; t < t1; ++t) {
@@ -342,8 +343,8 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
             const uint32_t ncnt = min(S, track_body(p, nt) - ns0);
             const int nbuf = (stage_no + 1) & 1;
             fence_proxy_async();
-            mbar_arrive_expect_tx(&sm.bar[nbuf], ncnt * 64u);
-            bulk_g2s(stage_buf[nbuf], p.records + (p.offsets[nt] + ns0) * kRecF4, ncnt * 64u,
+            mbar_arrive_expect_tx(&sm.bar[nbuf], ncnt * kRecBytes);
+            bulk_g2s(stage_buf[nbuf], p.records + (p.offsets[nt] + ns0) * kRecF4, ncnt * kRecBytes,
                      &sm.bar[nbuf]);
           }
         }
@@ -687,7 +688,7 @@ FarMixedConfig far_mixed_choose(uint32_t n_omega, uint32_t n_dirs, uint32_t n_tr
 size_t far_mixed_workspace(int64_t total_steps, uint64_t n_points, int n_out, uint32_t n_snaps,
                            const FarMixedConfig &cfg) {
   size_t b = 256;                                                    // status word
-  b += ((size_t)total_steps * 64 + 255) / 256 * 256;                 // step records
+  b += ((size_t)total_steps * kRecBytes + 255) / 256 * 256;          // step records
   b += ((size_t)cfg.n_sub * n_out * n_snaps * n_points * 8 + 255) / 256 * 256;  // partials
   b += (size_t)cfg.grid * cfg.W * cfg.K * 8 * 32 * sizeof(float);   // compensated sums
   return b;
@@ -705,7 +706,7 @@ int launch_far_mixed(FarMixedParams p, const FarMixedConfig &cfg, void *ws, size
   size_t off = 256;
   p.status = (int *)w;
   p.records = (float4 *)(w + off);
-  off += ((size_t)p.total_steps * 64 + 255) / 256 * 256;
+  off += ((size_t)p.total_steps * kRecBytes + 255) / 256 * 256;
   p.partial = (double *)(w + off);
   off += ((size_t)cfg.n_sub * p.n_out * p.n_snaps * P * 8 + 255) / 256 * 256;
   p.outer = (float *)(w + off);

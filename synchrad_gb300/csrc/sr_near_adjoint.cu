@@ -38,7 +38,7 @@ constexpr int kNASteps = kNAW * 32;   // steps per work item (one per lane)
 constexpr int kNAStage = 512;         // (screen point, omega) slots per constants stage
 constexpr int kNARS = 8;              // omega slots per phasor reseed
 constexpr int kNAG = 6;               // per-step gradient components: x (3), beta (3)
-constexpr int kNARecS = kRecF4 + 1;   // record stride in shared memory (conflict-free)
+constexpr int kNARecS = kRecF4;       // record stride in shared memory (80 bytes, as in HBM)
 constexpr int kNAPair = 11;           // float4 per pair of slots in the constants
 
 struct NearAdjParams {
@@ -203,15 +203,11 @@ __global__ void __launch_bounds__(W * 32, 2) nadj_kernel(NearAdjParams a) {
     const uint32_t r1 = min(n_body, r0 + kNASteps);
     const uint32_t has_prev = r0 > 0 ? 1u : 0u;
     const uint32_t n_rec = r1 - r0 + has_prev;
-    if (warp == 0) {  // one 64-byte bulk copy per record, spread over the lanes
-      if (lane == 0) {
-        fence_proxy_async();
-        mbar_arrive_expect_tx(&sm.bar, n_rec * 64u);
-      }
-      __syncwarp();
-      const float4 *src = p.records + (base + r0 - has_prev) * kRecF4;
-      for (uint32_t i = lane; i < n_rec; i += 32)
-        bulk_g2s(sm.rec[i], src + (uint64_t)i * kRecF4, 64u, &sm.bar);
+    if (threadIdx.x == 0) {  // the item's records in one bulk copy
+      fence_proxy_async();
+      mbar_arrive_expect_tx(&sm.bar, n_rec * kRecBytes);
+      bulk_g2s(sm.rec[0], p.records + (base + r0 - has_prev) * kRecF4, n_rec * kRecBytes,
+               &sm.bar);
     }
     const bool ok = mbar_wait_bounded(&sm.bar, it_no & 1u, kWaitLimitNs);
     if (__syncthreads_or(!ok)) {
@@ -439,7 +435,7 @@ NearAdjLayout nadj_layout(int64_t total_steps, uint64_t P, uint32_t n_omega, uin
   NearAdjLayout l;
   l.w_chunks = adj_weight_chunks(P, n_tracks, device_sm_count());
   l.records = 256;
-  l.gsf = l.records + up((size_t)total_steps * 64);
+  l.gsf = l.records + up((size_t)total_steps * kRecBytes);
   l.wtab = l.gsf + up((size_t)P * 4);
   l.sctab = l.wtab + up((size_t)n_omega * 16);
   l.glob = l.sctab + up((size_t)n_scr * 16);

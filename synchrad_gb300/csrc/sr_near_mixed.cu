@@ -57,7 +57,7 @@ __global__ void near_prepass_kernel(FarMixedParams p) {
     float4 *rec = p.records + g * kRecF4;
     if (s + 1 >= n) {
       const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-      rec[0] = zero; rec[1] = zero; rec[2] = zero; rec[3] = zero;
+      rec[0] = zero; rec[1] = zero; rec[2] = zero; rec[3] = zero; rec[4] = zero;
       continue;
     }
     const double time = (double)(uint32_t)(p.it_start[t] + (uint32_t)s) * p.dt;
@@ -73,6 +73,7 @@ __global__ void near_prepass_kernel(FarMixedParams p) {
     rec[1] = make_float4(dy.hi, dy.lo, dz.hi, dz.lo);
     rec[2] = make_float4((float)(ux * gi), (float)(uy * gi), (float)(uz * gi), (float)omb);
     rec[3] = make_float4(0.f, 0.f, 0.f, 0.f);
+    rec[4] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
 }
 
@@ -185,8 +186,9 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
       const uint32_t cnt = min((uint32_t)kStage, track_body(p, cur_t));
       const int b = stage_no & 1;
       fence_proxy_async();
-      mbar_arrive_expect_tx(&sm.bar[b], cnt * 64u);
-      bulk_g2s(sm.stage[b], p.records + (p.offsets[cur_t]) * kRecF4, cnt * 64u, &sm.bar[b]);
+      mbar_arrive_expect_tx(&sm.bar[b], cnt * kRecBytes);
+      bulk_g2s(sm.stage[b], p.records + (p.offsets[cur_t]) * kRecF4, cnt * kRecBytes,
+               &sm.bar[b]);
     }
 
     for (uint32_t t = t0; t < t1; ++t) {
@@ -332,8 +334,8 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
             const uint32_t ncnt = min((uint32_t)kStage, track_body(p, nt) - ns0);
             const int nbuf = (stage_no + 1) & 1;
             fence_proxy_async();
-            mbar_arrive_expect_tx(&sm.bar[nbuf], ncnt * 64u);
-            bulk_g2s(sm.stage[nbuf], p.records + (p.offsets[nt] + ns0) * kRecF4, ncnt * 64u,
+            mbar_arrive_expect_tx(&sm.bar[nbuf], ncnt * kRecBytes);
+            bulk_g2s(sm.stage[nbuf], p.records + (p.offsets[nt] + ns0) * kRecF4, ncnt * kRecBytes,
                      &sm.bar[nbuf]);
           }
         }
@@ -591,7 +593,7 @@ void launch_near_prepass(const FarMixedParams &p, int blocks, cudaStream_t strea
 size_t near_mixed_workspace(int64_t total_steps, uint64_t n_points, int n_out, uint32_t n_snaps,
                             const FarMixedConfig &cfg) {
   size_t b = 256;
-  b += ((size_t)total_steps * 64 + 255) / 256 * 256;
+  b += ((size_t)total_steps * kRecBytes + 255) / 256 * 256;
   b += ((size_t)cfg.n_sub * n_out * n_snaps * n_points * 8 + 255) / 256 * 256;
   b += (size_t)cfg.grid * cfg.W * cfg.K * kNOuter * 32 * sizeof(float);
   return b;
@@ -609,7 +611,7 @@ int launch_near_mixed(FarMixedParams p, const FarMixedConfig &cfg, void *ws, siz
   size_t off = 256;
   p.status = (int *)w;
   p.records = (float4 *)(w + off);
-  off += ((size_t)p.total_steps * 64 + 255) / 256 * 256;
+  off += ((size_t)p.total_steps * kRecBytes + 255) / 256 * 256;
   p.partial = (double *)(w + off);
   off += ((size_t)cfg.n_sub * p.n_out * p.n_snaps * P * 8 + 255) / 256 * 256;
   p.outer = (float *)(w + off);

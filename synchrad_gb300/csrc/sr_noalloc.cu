@@ -79,7 +79,7 @@ extern "C" int sr_spectrum_noalloc(const sr_tracks *t, const sr_grid *g, int com
   if (fixed + per_cta > kScratchBytes)
     return fail(SR_ERR_INVALID,
                 "sr_spectrum_noalloc: these sizes need %zu bytes of scratch, the static array "
-                "holds %zu (64 B per track step plus 8 B per point, output and snapshot)",
+                "holds %zu (80 B per track step plus 8 B per point, output and snapshot)",
                 fixed + per_cta, kScratchBytes);
   uint64_t grid = (kScratchBytes - fixed) / per_cta;
   if (grid > (uint64_t)cfg.grid) grid = (uint64_t)cfg.grid;
