@@ -489,9 +489,15 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
                 const uint32_t s = s0 + c0 + i;
                 const bool all_in = wabs_max * adt < kPiLo;
                 const bool all_out = wabs_min * adt > kPiHi;
-                // one masked path for every lane of the warp (excluded lanes
-                // carry a zero mask); skipped only when the whole warp is out
-                if (!__all_sync(0xffffffffu, all_out || nv == 0)) {
+                if (__all_sync(0xffffffffu, uniform && (all_in || nv == 0))) {
+                  // every point of the warp included: the straight-line step
+                  // (the same products as the masked path with a full mask)
+                  float2 zr, zi;
+                  step_seed(st, zr, zi);
+                  step_fast(st, zr, zi);
+                } else if (!__all_sync(0xffffffffu, all_out || nv == 0)) {
+                  // one masked path for every lane of the warp (excluded lanes
+                  // carry a zero mask); skipped only when the whole warp is out
                   const float4 A = st[0], AT = st[1 * 32], R2 = st[2 * 32], X = st[3 * 32],
                                Y = st[4 * 32];
                   uint32_t mask = (all_out || nv == 0) ? 0u : 0xffffffffu;
