@@ -52,6 +52,7 @@ namespace {
 //   r1 = (y.hi, y.lo, z.hi, z.lo)
 //   r2 = (bbar_x, bbar_y, bbar_z, 1 - bbar_z)
 //   r3 = (a_x, a_y, a_z, 0)
+//   r4 = 0 (padding: an 80-byte record stride spreads per-lane reads over the banks)
 // with beta = u / sqrt(1 + u.u) at s and s+1, a = (beta_{s+1} - beta_s)/dt,
 // bbar their mean (synchrad/kernel_farfield.cl:74-83), and 1 - beta_z formed
 // as (1 + ux^2 + uy^2) / (gamma (gamma + uz)) to avoid cancellation.
@@ -100,6 +101,7 @@ __global__ void far_prepass_kernel(FarMixedParams p) {
                          (float)(0.5 * (b1[2] + b0[2])), (float)(0.5 * (omb[0] + omb[1])));
     rec[3] = make_float4((float)((b1[0] - b0[0]) * dtInv), (float)((b1[1] - b0[1]) * dtInv),
                          (float)((b1[2] - b0[2]) * dtInv), 0.f);
+    rec[4] = make_float4(0.f, 0.f, 0.f, 0.f);  // padding
   }
 }
 

@@ -38,7 +38,7 @@ constexpr int kNSetupF4 = 8;    // float4 per (screen point, step) in the setup
 //   r1 = (y.hi, y.lo, z.hi, z.lo)
 //   r2 = (beta_x, beta_y, beta_z, 1 - beta_z) at step s
 //        (synchrad/kernel_nearfield.cl:79-82), 1 - beta_z = (1+ux^2+uy^2)/(gamma(gamma+uz))
-//   r3 = 0
+//   r3 = r4 = 0 (padding: an 80-byte record stride spreads per-lane reads over the banks)
 template <typename TT>
 __global__ void near_prepass_kernel(FarMixedParams p) {
   const TT *X = (const TT *)p.x, *Y = (const TT *)p.y, *Z = (const TT *)p.z;
@@ -434,9 +434,15 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
                 const uint32_t s = s0 + c0 + i;
                 const bool all_in = wabs_max * adt < kPiLo;
                 const bool all_out = wabs_min * adt > kPiHi;
-                // one masked path for every lane of the warp (excluded lanes
-                // carry a zero mask); skipped only when the whole warp is out
-                if (!__all_sync(0xffffffffu, all_out || nv == 0)) {
+                if (__all_sync(0xffffffffu, uniform && (all_in || nv == 0))) {
+                  // every point of the warp included: the straight-line step
+                  // (the same products as the masked path with a full mask)
+                  float2 zr, zi;
+                  step_seed(st, zr, zi);
+                  step_fast(st, zr, zi);
+                } else if (!__all_sync(0xffffffffu, all_out || nv == 0)) {
+                  // one masked path for every lane of the warp (excluded lanes
+                  // carry a zero mask); skipped only when the whole warp is out
                   const float4 A = st[0], F1 = st[1 * 32], F2 = st[2 * 32], F3 = st[3 * 32],
                                R2 = st[4 * 32], X = st[5 * 32], Y = st[6 * 32];
                   uint32_t mask = (all_out || nv == 0) ? 0u : 0xffffffffu;
