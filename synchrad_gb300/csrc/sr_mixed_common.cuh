@@ -11,7 +11,7 @@ constexpr int kStage = 128;         // steps per TMA stage
 constexpr int kFoldStages = 8;      // FP32 sums fold into compensated pairs every 1024 steps
 // float4 per step record: 64 bytes of data and 16 of padding, so that 32
 // lanes reading one record each from shared memory hit every bank once per
-// quarter warp (at a 64-byte stride two lanes in eight share the same banks)
+// quarter warp (at a 64-byte stride four lanes in eight share the same banks)
 constexpr int kRecF4 = 5;
 constexpr uint32_t kRecBytes = kRecF4 * 16;
 constexpr float kPiLo = 3.14159265358979f * (1.0f - 4e-6f);
