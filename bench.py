@@ -179,6 +179,29 @@ def executed_flops_per_unit(w):
     return 30 if w.args.get("mode", "far") == "near" else FLOPS_PER_UNIT
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the
+# dominant kernel in an ncu capture of 16 tracks of the same workload, and the
+# point-steps of that launch.  With the same steps per track the traffic (the
+# per-track partial-spectrum updates and the step records) grows with the
+# number of tracks, as the point-steps do, so a launch's traffic is this
+# ratio times its point-steps.
+NCU_TRAFFIC = {
+    "far": (175.7e6 + 212.3e6, 16 * 3999 * 512 * 64 * 64, "far_mixed_kernel<32,8>"),
+    "near": (50.4e6 + 20.3e6, 16 * 7999 * 256 * 64 * 64, "near_mixed_kernel<8>"),
+}
+
+
+def launch_traffic(workload, args, pt_steps):
+    """DRAM bytes per launch scaled from the ncu capture, or None where the
+    capture does not describe this workload (other steps per track or grid)."""
+    if workload not in NCU_TRAFFIC or args.track_steps is not None or args.grid is not None:
+        return None, None
+    nbytes, units, src = NCU_TRAFFIC[workload]
+    return (nbytes * pt_steps / units,
+            f"ncu capture of one 16-track launch of {src} (dram__bytes_read.sum + "
+            "dram__bytes_write.sum), scaled by point-steps")
+
+
 def cpu_sample(w, n_tracks=4, sub=(16, 16)):
     """A bounded sample of the workload for the CPU oracle: the first tracks on
     the full omega axis and a sub-grid of directions."""
@@ -527,9 +550,11 @@ def main():
     peak = max(tf_s.value, tf_p.value)
     clk = clocks.summary()
     kname = "near_mixed_kernel" if mode == "near" else "far_mixed_kernel"
+    traffic, traffic_src = launch_traffic(args.workload, args, pt_steps)
     roofline = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak if peak else None,
-                "traffic": None,
+                "traffic": traffic, "traffic_unit": "bytes per launch",
+                "traffic_source": traffic_src,
                 "kernel": (f"{kname} ({shape['points_per_lane']} omega points per lane, "
                            f"{shape['lanes_per_direction']} lanes per direction, 8 warps per CTA)"),
                 "kernel_ms_avg": kern_avg_ms,
