@@ -38,7 +38,8 @@ class GoldenCase:
 
 
 def names():
-    return sorted(p.stem for p in GOLDEN.glob("*.npz"))
+    """The spectrum cases (host_golden.npz holds the host-logic vectors)."""
+    return sorted(p.stem for p in GOLDEN.glob("*.npz") if p.stem != "host_golden")
 
 
 def load(name: str) -> GoldenCase:
