@@ -1,9 +1,11 @@
 """Generate the golden vectors in tests/golden/*.npz.
 
 Each case is a full ``SynchRad(args).calculate_spectrum(tracks, ...)`` call
-evaluated by the reference's own kernel source compiled for the CPU
-(``oracle/_ref``, built by ``oracle/build_ref.sh`` from the reference tree)
-with the reference's host logic restated in ``oracle/host.py``.  The inputs
+run by the reference's own host code (``ref_host_flow.py``: the body of
+``synchrad/calc.py`` parsed from the reference tree) on the reference's own
+kernel source compiled for the CPU (``oracle/_ref``, built by
+``oracle/build_ref.sh``).  Every case is also run through the oracle's host
+restatement (``oracle/host.py``) and must agree bit for bit.  The inputs
 (tracks, grid, call arguments) are stored next to the outputs so the GPU
 parity tests can replay them without regenerating anything.
 
@@ -24,6 +26,9 @@ sys.path.insert(0, str(ROOT))
 
 import oracle  # noqa: E402
 from oracle import host  # noqa: E402
+
+sys.path.insert(0, str(Path(__file__).resolve().parent))
+import ref_host_flow  # noqa: E402
 from synchrad_gb300 import workloads as wl  # noqa: E402
 
 OUT = Path(__file__).resolve().parent
@@ -131,8 +136,14 @@ def main(only=()):
         if only and not any(name.startswith(o) for o in only):
             continue
         call = dict(kw)
-        rad, tw, snaps, a = host.calculate_spectrum(
-            args, [list(t) for t in tracks], kind="ref", nthreads=4, **call)
+        rad, tw, snaps, a = ref_host_flow.calculate_spectrum(
+            dict(args), [list(t) for t in tracks], **call)
+        o_rad, o_tw, o_snaps, _ = host.calculate_spectrum(
+            dict(args), [list(t) for t in tracks], kind="ref", nthreads=4, **call)
+        assert sorted(o_rad) == sorted(rad) and o_tw == tw, name
+        assert np.array_equal(np.asarray(o_snaps), np.asarray(snaps)), name
+        for key in rad:
+            assert np.array_equal(o_rad[key], rad[key]), (name, key)
         data = {}
         for i, t in enumerate(tracks):
             for j, key in enumerate(("x", "y", "z", "ux", "uy", "uz")):
