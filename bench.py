@@ -58,6 +58,8 @@ def parse():
                          "betatron tracks of 500-20000 steps; adjoint: forward and "
                          "backward of sum(g * S) for 256 tracks x 2000 steps on 128 x 32 x 32")
     ap.add_argument("--tracks", type=int, default=None)
+    ap.add_argument("--seed", type=int, default=0,
+                    help="seed of the synthetic tracks (numpy default_rng)")
     ap.add_argument("--track-steps", type=int, default=None)
     ap.add_argument("--grid", type=int, nargs=3, default=None)
     ap.add_argument("--e2e-steps", type=int, default=None)
@@ -140,7 +142,7 @@ class ClockSampler:
 
 def make_workload(args):
     from synchrad_gb300 import workloads as wl
-    kw = {}
+    kw = {"seed": args.seed}
     if args.tracks is not None:
         kw["n_tracks"] = args.tracks
     if args.grid is not None:
@@ -404,7 +406,7 @@ def adjoint_main(args):
                 "vs_baseline": None,
                 "dtype": "f32 (mixed: double-float phase, FP32 sums, FP64 gradients)",
                 "data": "synthetic",
-                "config": {"workload": w.name, "n_tracks": len(w.tracks),
+                "config": {"workload": w.name, "n_tracks": len(w.tracks), "seed": args.seed,
                            "steps_per_track": int(lengths[0]), "grid": [nO, nT, nP],
                            "pt_steps_per_step": pt_steps,
                            "loss": loss_name,
@@ -651,7 +653,7 @@ def main():
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32 (mixed: double-float phase, compensated FP32 sums, FP64 spectrum)",
                 "data": "synthetic",
-                "config": {"workload": w.name, "n_tracks": len(w.tracks),
+                "config": {"workload": w.name, "n_tracks": len(w.tracks), "seed": args.seed,
                            "steps_per_track": (int(w.pt_steps // P // len(w.tracks)) + 1
                                                if args.workload != "ragged" else "500-20000"),
                            "grid": list(w.args["grid"][-1]),
