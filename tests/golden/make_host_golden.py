@@ -2,7 +2,10 @@
 (``SynchRad._init_args``, synchrad/calc.py:355-451), result arrays and
 FormFactor (``_init_raditaion``, :453-484), device axes (``_init_data``,
 :486-512), snapshot iterations (``_set_snap_iterations``, :626-630) and the
-``Utilities`` post-processing (synchrad/utils.py:21-166).
+``Utilities`` post-processing (synchrad/utils.py:21-166), and the HDF5
+layout ``calculate_spectrum`` writes (synchrad/calc.py:274-290), recorded
+through ``tests/fake_h5py.py`` while the reference's host flow
+(``ref_host_flow.py``) runs on its CPU-built kernels.
 
 The reference package cannot be imported here (it needs pyopencl, mako and
 h5py), so this script runs the reference's own function bodies: it parses
@@ -135,6 +138,80 @@ def ref_args(RefCalc, args):
     return obj
 
 
+# (grid case, calculate_spectrum arguments) of the HDF5-layout cases; a
+# "file_tracks" entry names a track file written by write_track_file
+H5_CASES = [
+    ("far_double", {"comp": "cartesian", "nSnaps": 2, "it_range": [0, 60],
+                    "sigma_particle": 1e-5, "weights_normalize": "mean"}),
+    ("near_float_log", {"comp": "total", "nSnaps": 1, "L_screen": 1000.0,
+                        "weights_normalize": "ones", "Np_max": 2}),
+    ("far_log", {"comp": "spheric_complex", "nSnaps": 1}),
+    ("far_double", {"comp": "total", "nSnaps": 3, "file_tracks": "tracks_with_range"}),
+    ("far_double", {"comp": "total", "nSnaps": 2, "Np_max": 2,
+                    "file_tracks": "tracks_without_range"}),
+]
+
+
+def write_track_file(h5, name, tracks, dt, it_range=None):
+    """A track file in the layout the reference's converters write and
+    calculate_spectrum reads (synchrad/calc.py:186-219): misc/cdt,
+    misc/N_particles, optionally misc/it_range, tracks/<i>/<x..it_start>."""
+    f = h5.File(name, "w")
+    f["misc/cdt"] = dt
+    f["misc/N_particles"] = len(tracks)
+    if it_range is not None:
+        f["misc/it_range"] = np.asarray(it_range)
+    for i, t in enumerate(tracks):
+        for c, v in zip(("x", "y", "z", "ux", "uy", "uz", "w", "it_start"), t):
+            f[f"tracks/{i}/{c}"] = v
+    f.close()
+
+
+def prepare_track_files(h5, tracks, dt):
+    write_track_file(h5, "tracks_with_range", tracks, dt, it_range=(0, 40))
+    write_track_file(h5, "tracks_without_range", tracks, dt)
+
+
+def h5_tracks():
+    """Three short undulator tracks (8-element lists, it_start 0, 3, 5)."""
+    sys.path.insert(0, str(Path(__file__).resolve().parents[2]))
+    from synchrad_gb300 import workloads as wl
+    tracks, dt, _ = wl.analytic_undulator_tracks(n_particles=3, n_periods=1,
+                                                 steps_per_period=16, seed=5)
+    out = []
+    for i, t in enumerate(tracks):
+        out.append([np.asarray(a)[:30 + 5 * i].copy() for a in t[:6]] + [0.5 + 0.5 * i, 2 * i])
+    return out, dt
+
+
+def record_h5(data, meta):
+    sys.path.insert(0, str(Path(__file__).resolve().parent))
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+    import fake_h5py
+    import ref_host_flow
+    tracks, dt = h5_tracks()
+    prepare_track_files(fake_h5py, tracks, dt)
+    meta["h5_cases"] = []
+    for i, (gname, call) in enumerate(H5_CASES):
+        name = f"h5case{i}"
+        in_tracks = [] if "file_tracks" in call else [list(t) for t in tracks]
+        step = None if "file_tracks" in call else dt
+        ref_host_flow.calculate_spectrum(dict(GRID_CASES[gname]), in_tracks,
+                                         h5py_module=fake_h5py, timeStep=step,
+                                         file_spectrum=name, **call)
+        store = fake_h5py.FILES.pop(name)
+        paths = sorted(store)
+        for path in paths:
+            v = store[path]
+            if path.startswith("radiation/"):
+                data[f"h5/{i}/{path}"] = np.array(list(v.shape) + [v.dtype.itemsize])
+            else:
+                data[f"h5/{i}/{path}"] = (np.array(v.decode()) if isinstance(v, bytes)
+                                          else np.asarray(v))
+        meta["h5_cases"].append({"grid": gname, "call": call, "paths": paths,
+                                 "dt": float(dt)})
+
+
 def main():
     RefCalc = load_calc_functions()
     Utilities = load_utilities()
@@ -208,6 +285,7 @@ def main():
             data[f"util/{ci}/out/{cname}"] = np.asarray(fn())
         meta["utility_cases"].append({"grid": gname, "comp": comp, "keys": keys,
                                       "calls": sorted(calls)})
+    record_h5(data, meta)
     data["meta_json"] = np.array(json.dumps(meta))
     np.savez_compressed(OUT, **data)
     print(f"{OUT.name}: {len(data) - 1} arrays")

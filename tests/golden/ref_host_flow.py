@@ -117,14 +117,16 @@ def _load_class():
 _CLASS = None
 
 
-def calculate_spectrum(args: dict, tracks, **call):
+def calculate_spectrum(args: dict, tracks, h5py_module=None, **call):
     """``SynchRad(args).calculate_spectrum(tracks, **call)`` by the reference's
     host code and kernels.  Returns ``(radiation, total_weight,
     snap_iterations, Args)``; ``tracks`` is used as given (the reference
-    normalises weights in place)."""
+    normalises weights in place).  ``h5py_module`` serves the reference's
+    ``h5py`` calls when ``file_spectrum`` is given."""
     global _CLASS
     if _CLASS is None:
         _CLASS = _load_class()
+    _CLASS.calculate_spectrum.__globals__["h5py"] = h5py_module
     if not oracle.ref_available():
         raise RuntimeError("oracle/_ref is not buildable here (reference tree missing)")
     obj = _CLASS()
