@@ -60,3 +60,61 @@ def test_pack_tracks_rejects_empty_track():
     tr = [[np.zeros(0) for _ in range(6)] + [1.0, 0]]
     with pytest.raises(ValueError):
         pack_tracks(tr, np.float64, 1, 0.1, device="cpu", pinned=False)
+
+
+def _header_signatures():
+    """{name: (return kind, [parameter kinds])} parsed from the header, kinds
+    being 'ptr' or the C scalar type."""
+    import re
+    text = (ROOT / "include" / "synchrad_gb300.h").read_text()
+    text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+    sigs = {}
+    for m in re.finditer(r"(int|int64_t|void|const char \*)\s*(sr_\w+)\s*\(([^;{]*?)\)\s*;",
+                         text, re.S):
+        ret, name, params = m.group(1), m.group(2), " ".join(m.group(3).split())
+        kinds = []
+        if params and params != "void":
+            for p in params.split(","):
+                p = p.strip()
+                if "*" in p:
+                    kinds.append("ptr")
+                else:
+                    kinds.append(" ".join(p.replace("const ", "").split()[:-1]))
+        sigs[name] = ("ptr" if "*" in ret else ret, kinds)
+    return sigs
+
+
+def _ctypes_kind(t):
+    import ctypes
+    if t is None:
+        return "void"
+    if t in (ctypes.c_void_p, ctypes.c_char_p) or hasattr(t, "_type_") and isinstance(
+            getattr(t, "_type_", None), type):
+        return "ptr"
+    size_t = ctypes.c_size_t
+    table = {ctypes.c_int: "int", ctypes.c_int64: "int64_t", ctypes.c_uint32: "uint32_t",
+             ctypes.c_double: "double", size_t: "size_t"}
+    for k, v in table.items():
+        if t is k:
+            return v
+    return repr(t)
+
+
+def test_binding_signatures_match_header():
+    """Every ctypes argtypes/restype agrees with the header prototype: number
+    of parameters, pointer or scalar, and the scalar's C type (size_t and the
+    64-bit integers are the same width here, so size_t is checked by name)."""
+    from synchrad_gb300 import _lib
+    L = _lib.lib()
+    sigs = _header_signatures()
+    assert sorted(sigs) == sorted(_lib.EXPORTS)
+    for name, (ret, params) in sigs.items():
+        f = getattr(L, name)
+        assert _ctypes_kind(f.restype) == ret, (name, f.restype, ret)
+        got = [_ctypes_kind(a) for a in f.argtypes]
+        assert len(got) == len(params), (name, got, params)
+        for i, (g, p) in enumerate(zip(got, params)):
+            if p == "size_t":
+                assert g in ("size_t", "int64_t"), (name, i, g, p)
+            else:
+                assert g == p, (name, i, g, p)
