@@ -235,6 +235,33 @@ def time_cpu_oracle(w, nthreads, n_tracks=4, sub=(16, 16), kind=None):
     return pts / el / 1e9, el, pts, kind
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the machine)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.machine()
+
+
+def single_core_baseline(w, kind=None):
+    """The oracle on one thread over a smaller sample of the same workload."""
+    v1, el1, _, kind = time_cpu_oracle(w, 1, n_tracks=1, sub=(8, 8), kind=kind)
+    return {"value": v1, "unit": UNIT, "cores": 1, "kind": kind,
+            "sample": (f"first track on the full omega axis x 8 x 8 directions or screen "
+                       f"points, FP64, 1 thread, {el1:.1f} s")}
+
+
 def reference_arm(args):
     """--impl reference: the reference's CPU implementation of the path."""
     ws, rank, _ = dist_env()
@@ -259,7 +286,8 @@ def reference_arm(args):
             "config": {"workload": w.name, "sample": sample},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": nth,
                              "kind": "reference" if kind == "reference" else "port",
-                             "sample": sample},
+                             "sample": sample, "model": cpu_model(),
+                             "single_core": single_core_baseline(w, kind)},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -645,7 +673,8 @@ def main():
         v, el, pts, kind = time_cpu_oracle(w, nth)
         cpu = {"value": v, "unit": UNIT, "cores": nth, "kind": kind,
                "sample": f"first 4 tracks on the full omega axis x 16 x 16 directions or "
-                         f"screen points, FP64, {nth} threads, {el:.1f} s"}
+                         f"screen points, FP64, {nth} threads, {el:.1f} s",
+               "model": cpu_model(), "single_core": single_core_baseline(w, kind)}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,

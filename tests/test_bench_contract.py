@@ -37,6 +37,9 @@ def test_reference_arm_prints_one_contract_line():
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["unit"] == d["unit"] and cb["cores"] >= 1
     assert cb["kind"] in ("reference", "port") and cb["sample"]
+    assert cb["model"]
+    one = cb["single_core"]
+    assert one["cores"] == 1 and one["value"] > 0 and one["unit"] == d["unit"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}
 
