@@ -21,11 +21,9 @@ def directions(sinT, cosT, sinP, cosP):
     return n0, n1, n2
 
 
-def far_total_torch(x, y, z, ux, uy, uz, w, offsets, dt, omega, sinT, cosT, sinP, cosP):
-    """Spectrum [nPhi, nTheta, nOmega] of the concatenated tracks (CSR ``offsets``)."""
-    n0, n1, n2 = directions(sinT, cosT, sinP, cosP)
-    N = torch.stack([n0, n1, n2], -1)
-    S = torch.zeros(N.shape[0], omega.numel(), dtype=torch.float64, device=x.device)
+def _far_track_sums(x, y, z, ux, uy, uz, offsets, dt, omega, N, n0, n1, n2):
+    """Per track: (t, re, im) with re/im [nDir, nOmega, 3] the Cartesian
+    components of the masked sum (synchrad/kernel_farfield.cl:59-107)."""
     for t in range(len(offsets) - 1):
         a0, a1 = int(offsets[t]), int(offsets[t + 1])
         if a1 - a0 < 2:
@@ -50,5 +48,43 @@ def far_total_torch(x, y, z, ux, uy, uz, w, offsets, dt, omega, sinT, cosT, sinP
         sw = torch.where(mask, torch.sin(phase), torch.zeros_like(phase))
         re = torch.einsum("mdo,mdk->dok", cw, amp)
         im = torch.einsum("mdo,mdk->dok", sw, amp)
+        yield t, re, im
+
+
+def far_total_torch(x, y, z, ux, uy, uz, w, offsets, dt, omega, sinT, cosT, sinP, cosP):
+    """Spectrum [nPhi, nTheta, nOmega] of the concatenated tracks (CSR ``offsets``)."""
+    n0, n1, n2 = directions(sinT, cosT, sinP, cosP)
+    N = torch.stack([n0, n1, n2], -1)
+    S = torch.zeros(N.shape[0], omega.numel(), dtype=torch.float64, device=x.device)
+    for t, re, im in _far_track_sums(x, y, z, ux, uy, uz, offsets, dt, omega, N, n0, n1, n2):
         S = S + w[t] * dt * dt * ((re * re).sum(-1) + (im * im).sum(-1))
     return S.reshape(sinP.numel(), sinT.numel(), omega.numel())
+
+
+def far_comps_torch(x, y, z, ux, uy, uz, w, offsets, dt, omega, sinT, cosT, sinP, cosP,
+                    comp="cartesian"):
+    """Per-component spectra [3][nPhi, nTheta, nOmega]: 'cartesian' |A_x|^2,
+    |A_y|^2, |A_z|^2 (synchrad/kernel_farfield.cl:166-223) or 'spheric'
+    |A_r|^2, |A_theta|^2, |A_phi|^2 on r = n, theta-hat = (cos theta cos phi,
+    cos theta sin phi, -sin theta), phi-hat = (-sin phi, cos phi, 0)
+    (:382-388, 442-445), each times w dt^2 and summed over tracks."""
+    n0, n1, n2 = directions(sinT, cosT, sinP, cosP)
+    N = torch.stack([n0, n1, n2], -1)
+    if comp == "cartesian":
+        basis = torch.eye(3, dtype=torch.float64, device=x.device)[None].expand(N.shape[0], 3, 3)
+    elif comp == "spheric":
+        cT = cosT[None, :].expand(sinP.numel(), sinT.numel()).reshape(-1)
+        sT = sinT[None, :].expand(sinP.numel(), sinT.numel()).reshape(-1)
+        cP = cosP[:, None].expand(sinP.numel(), sinT.numel()).reshape(-1)
+        sP = sinP[:, None].expand(sinP.numel(), sinT.numel()).reshape(-1)
+        th = torch.stack([cT * cP, cT * sP, -sT], -1)
+        ph = torch.stack([-sP, cP, torch.zeros_like(sP)], -1)
+        basis = torch.stack([N, th, ph], 1)  # [nDir, comp, xyz]
+    else:
+        raise ValueError(comp)
+    S = torch.zeros(3, N.shape[0], omega.numel(), dtype=torch.float64, device=x.device)
+    for t, re, im in _far_track_sums(x, y, z, ux, uy, uz, offsets, dt, omega, N, n0, n1, n2):
+        pr = torch.einsum("dok,dck->cdo", re, basis)
+        pi = torch.einsum("dok,dck->cdo", im, basis)
+        S = S + w[t] * dt * dt * (pr * pr + pi * pi)
+    return S.reshape(3, sinP.numel(), sinT.numel(), omega.numel())
