@@ -12,11 +12,9 @@ import math
 import torch
 
 
-def near_total_torch(x, y, z, ux, uy, uz, w, offsets, dt, omega, radius, sinP, cosP, L_screen):
-    """Spectrum [nPhi, nR, nOmega] of the concatenated tracks (CSR ``offsets``)."""
-    X0 = (radius[None, :] * cosP[:, None]).reshape(-1)  # screen point index iPhi * nR + iR
-    Y0 = (radius[None, :] * sinP[:, None]).reshape(-1)
-    S = torch.zeros(X0.numel(), omega.numel(), dtype=torch.float64, device=x.device)
+def _near_track_sums(x, y, z, ux, uy, uz, offsets, dt, omega, X0, Y0, L_screen):
+    """Per track: (t, re, im) with re/im [nScreen, nOmega, 3] the Cartesian
+    components of the masked sum (synchrad/kernel_nearfield.cl:58-102)."""
     for t in range(len(offsets) - 1):
         a0, a1 = int(offsets[t]), int(offsets[t + 1])
         if a1 - a0 < 2:
@@ -44,5 +42,32 @@ def near_total_torch(x, y, z, ux, uy, uz, w, offsets, dt, omega, radius, sinP, c
               - omega[None, :, None] * torch.einsum("mdo,mdk->dok", sw, c1b))
         im = (torch.einsum("mdo,mdk->dok", sw, c2)
               + omega[None, :, None] * torch.einsum("mdo,mdk->dok", cw, c1b))
+        yield t, re, im
+
+
+def _screen(radius, sinP, cosP):
+    X0 = (radius[None, :] * cosP[:, None]).reshape(-1)  # screen point index iPhi * nR + iR
+    Y0 = (radius[None, :] * sinP[:, None]).reshape(-1)
+    return X0, Y0
+
+
+def near_total_torch(x, y, z, ux, uy, uz, w, offsets, dt, omega, radius, sinP, cosP, L_screen):
+    """Spectrum [nPhi, nR, nOmega] of the concatenated tracks (CSR ``offsets``)."""
+    X0, Y0 = _screen(radius, sinP, cosP)
+    S = torch.zeros(X0.numel(), omega.numel(), dtype=torch.float64, device=x.device)
+    for t, re, im in _near_track_sums(x, y, z, ux, uy, uz, offsets, dt, omega, X0, Y0,
+                                      L_screen):
         S = S + w[t] * dt * dt * ((re * re).sum(-1) + (im * im).sum(-1))
     return S.reshape(sinP.numel(), radius.numel(), omega.numel())
+
+
+def near_cartesian_torch(x, y, z, ux, uy, uz, w, offsets, dt, omega, radius, sinP, cosP,
+                         L_screen):
+    """Per-component spectra [3][nPhi, nR, nOmega]: w dt^2 |A_x|^2, |A_y|^2,
+    |A_z|^2 summed over tracks (synchrad/kernel_nearfield.cl:106-214)."""
+    X0, Y0 = _screen(radius, sinP, cosP)
+    S = torch.zeros(3, X0.numel(), omega.numel(), dtype=torch.float64, device=x.device)
+    for t, re, im in _near_track_sums(x, y, z, ux, uy, uz, offsets, dt, omega, X0, Y0,
+                                      L_screen):
+        S = S + w[t] * dt * dt * (re * re + im * im).permute(2, 0, 1)
+    return S.reshape(3, sinP.numel(), radius.numel(), omega.numel())

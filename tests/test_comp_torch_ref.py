@@ -1,10 +1,12 @@
-"""The float64 PyTorch restatement's per-component far-field spectra
-(``far_torch_ref.far_comps_torch``) against the oracle, on the CPU: the
-'cartesian' and 'spheric' spectra of the reference kernels
-(synchrad/kernel_farfield.cl:111-225, 346-469) and the autograd gradient of a
-component-weighted loss sum_c sum_p g_c S_c against fourth-order finite
-differences of the oracle.  Groundwork for adjoints of the component comps:
-the gradient the CUDA adjoint will be checked against."""
+"""The float64 PyTorch restatements' per-component spectra against the
+oracle, on the CPU: the far-field 'cartesian' and 'spheric' spectra
+(``far_torch_ref.far_comps_torch``; synchrad/kernel_farfield.cl:111-225,
+346-469) with the autograd gradient of a component-weighted loss
+sum_c sum_p g_c S_c against fourth-order finite differences of the oracle,
+and the near-field 'cartesian' spectra (``near_torch_ref.near_cartesian_torch``;
+synchrad/kernel_nearfield.cl:106-214).  Groundwork for adjoints of the
+component comps: the gradients a CUDA adjoint of those comps is checked
+against."""
 import numpy as np
 import pytest
 
@@ -73,3 +75,23 @@ def test_component_loss_gradient_matches_oracle_fd():
         got.append(float(ts[c].grad[offsets[t] + s]))
         exp.append(fd)
     assert rel_l2(got, exp) <= 1e-7
+
+
+def test_near_component_spectra_match_oracle():
+    import near_torch_ref as ntr
+    from test_near_adjoint import concat as nconcat, make_case as nmake_case
+    tracks, dt, axes, n, _, L, _ = nmake_case(True)
+    _, offsets, coords, weights = nconcat(tracks)
+    ts = [torch.tensor(c, dtype=torch.float64) for c in coords]
+    ax = [torch.tensor(a, dtype=torch.float64) for a in axes]
+    S = ntr.near_cartesian_torch(*ts, torch.tensor(weights), offsets, dt, *ax, L).numpy()
+    exp = 0
+    for t in tracks:
+        nst = t[0].size
+        spec = [np.zeros((n[2], n[1], n[0]), dtype=np.float64) for _ in range(3)]
+        oracle.run_track("port", "near", "cartesian", spec,
+                         [np.ascontiguousarray(a) for a in t[:6]], t[6], 0, nst, nst, axes, n,
+                         dt, np.array([nst], dtype=np.uint32), L_screen=L, nthreads=4)
+        exp = exp + np.stack(spec)
+    for c in range(3):
+        assert rel_l2(S[c], exp[c]) <= 1e-12, c
