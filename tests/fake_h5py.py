@@ -4,7 +4,8 @@ h5py is installed neither here nor on the GPU host, so the HDF5 code paths
 (spectrum output, ``Args`` round trip, track-file input) are exercised
 against this module: ``File(name, mode)`` opens a dict of absolute dataset
 paths kept in ``FILES``; ``f[path] = value`` stores a numpy copy,
-``f[path][()]`` reads it back, groups answer ``keys()`` with their children.
+``f[path][()]`` reads it back (``f[path][i, j]`` a slice of it, ``.shape`` its
+shape), groups answer ``keys()`` with their children.
 String values come back as ``bytes``, as h5py returns variable-length
 strings.
 """
@@ -34,7 +35,13 @@ class _Node:
             raise TypeError(f"{self._path} is a dataset")
         return self._children()
 
+    @property
+    def shape(self):
+        return np.shape(self._store[self._path])
+
     def __getitem__(self, key):
+        if not isinstance(key, str) and key != ():
+            return np.array(self._store[self._path][key])   # a slice of a dataset
         if key == ():
             if self._path not in self._store:
                 raise KeyError(self._path)

@@ -38,8 +38,9 @@ class GoldenCase:
 
 
 def names():
-    """The spectrum cases (host_golden.npz holds the host-logic vectors)."""
-    return sorted(p.stem for p in GOLDEN.glob("*.npz") if p.stem != "host_golden")
+    """The spectrum cases (the *_golden.npz files hold the host-logic and
+    converter vectors)."""
+    return sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.endswith("_golden"))
 
 
 def load(name: str) -> GoldenCase:
