@@ -130,7 +130,10 @@ int sr_spectrum(const sr_tracks *tracks, const sr_grid *grid, int comp,
 int sr_spectrum_noalloc(const sr_tracks *tracks, const sr_grid *grid, int comp,
                         void *const *out, void *stream);
 
-/* Scratch bytes sr_spectrum needs for these sizes (reads host fields only). */
+/* Scratch bytes sr_spectrum needs for these sizes (reads host fields only):
+ * 0 for SR_PREC_DOUBLE and SR_PREC_FLOAT*, which need none; SR_ERR_INVALID
+ * (negative, with a message) for NULL arguments, an unknown mode, comp or
+ * precision, or a spheric comp on a near-field grid. */
 int64_t sr_workspace_bytes(const sr_tracks *tracks, const sr_grid *grid,
                            int comp, int precision);
 

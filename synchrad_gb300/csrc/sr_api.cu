@@ -132,10 +132,17 @@ extern "C" int sr_version(void) { return 100; }
 
 extern "C" int64_t sr_workspace_bytes(const sr_tracks *t, const sr_grid *g, int comp,
                                       int precision) {
-  if (!t || !g) return -1;
-  if (precision != SR_PREC_MIXED) return 0;
+  clear_error();
+  if (!t || !g) return fail(SR_ERR_INVALID, "tracks and grid must not be NULL");
+  if (g->mode != SR_MODE_FAR && g->mode != SR_MODE_NEAR)
+    return fail(SR_ERR_INVALID, "unknown grid mode %u", g->mode);
   const int nout = n_outputs(comp);
-  if (nout == 0) return -1;
+  if (nout == 0) return fail(SR_ERR_INVALID, "unknown comp %d", comp);
+  if (g->mode == SR_MODE_NEAR && comp > SR_COMP_CARTESIAN_COMPLEX)
+    return fail(SR_ERR_INVALID, "comp %d is far-field only (spheric components)", comp);
+  if (precision < SR_PREC_DOUBLE || precision > SR_PREC_MIXED)
+    return fail(SR_ERR_INVALID, "unknown precision %d", precision);
+  if (precision != SR_PREC_MIXED) return 0;
   const uint64_t P = (uint64_t)g->n_omega * g->n_theta * g->n_phi;
   const FarMixedConfig cfg = mixed_config(t, g, comp);
   if (g->mode == SR_MODE_FAR)

@@ -118,3 +118,42 @@ def test_binding_signatures_match_header():
                 assert g in ("size_t", "int64_t"), (name, i, g, p)
             else:
                 assert g == p, (name, i, g, p)
+
+
+def test_argument_errors_are_reported_before_any_device_work():
+    """Invalid arguments come back as SR_ERR_INVALID with a message from the
+    host-side checks, without a CUDA call (so also on a machine without a GPU)."""
+    import ctypes
+    from synchrad_gb300 import _lib
+    L = _lib.lib()
+    t, g = _lib.SrTracks(), _lib.SrGrid()
+    t.n_tracks, t.total_steps, t.dtype = 1, 10, _lib.SR_DTYPE_F64
+    g.n_omega, g.n_theta, g.n_phi, g.dtype = 4, 2, 2, _lib.SR_DTYPE_F64
+    tp, gp = ctypes.byref(t), ctypes.byref(g)
+    cases = [
+        (lambda: L.sr_workspace_bytes(None, gp, 0, 3), "must not be NULL"),
+        (lambda: L.sr_workspace_bytes(tp, gp, 9, 3), "unknown comp"),
+        (lambda: L.sr_workspace_bytes(tp, gp, 0, 7), "unknown precision"),
+    ]
+    for fn, msg in cases:
+        assert fn() == _lib.SR_ERR_INVALID
+        assert msg in L.sr_last_error().decode()
+    g.mode = _lib.SR_MODE_NEAR
+    assert L.sr_workspace_bytes(tp, gp, 3, 3) == _lib.SR_ERR_INVALID
+    assert "far-field only" in L.sr_last_error().decode()
+    g.mode = 5
+    assert L.sr_workspace_bytes(tp, gp, 0, 3) == _lib.SR_ERR_INVALID
+    assert "unknown grid mode" in L.sr_last_error().decode()
+    g.mode = _lib.SR_MODE_FAR
+    assert L.sr_workspace_bytes(tp, gp, 0, _lib.SR_PREC_DOUBLE) == 0
+    assert L.sr_workspace_bytes(tp, gp, 0, _lib.SR_PREC_MIXED) > 0
+    # sr_spectrum: argument checks first
+    outs = (ctypes.c_void_p * 6)()
+    assert L.sr_spectrum(tp, gp, 0, 3, outs, None, 0, None) == _lib.SR_ERR_INVALID
+    assert "output array 0 is NULL" in L.sr_last_error().decode()
+    outs[0] = 256
+    assert L.sr_spectrum(tp, gp, 0, _lib.SR_PREC_FLOAT, outs, None, 0, None) == \
+        _lib.SR_ERR_INVALID
+    assert "FP32 tracks and grid" in L.sr_last_error().decode()
+    assert L.sr_spectrum(tp, gp, 0, 3, outs, None, 0, None) == _lib.SR_ERR_INVALID
+    assert "grid axis pointer is NULL" in L.sr_last_error().decode()
