@@ -39,8 +39,8 @@ std::mutex g_tmu;
 std::map<TuneKey, FarMixedConfig> g_cache;
 
 TuneKey key_of(const sr_tracks *t, const sr_grid *g, int comp) {
-  TuneKey k;
-  cudaGetDevice(&k.device);
+  TuneKey k{};
+  if (cudaGetDevice(&k.device) != cudaSuccess) k.device = -1;  // no device: one key space
   k.mode = g->mode;
   k.comp = comp;
   k.dtype = t->dtype;

@@ -157,3 +157,37 @@ def test_argument_errors_are_reported_before_any_device_work():
     assert "FP32 tracks and grid" in L.sr_last_error().decode()
     assert L.sr_spectrum(tp, gp, 0, 3, outs, None, 0, None) == _lib.SR_ERR_INVALID
     assert "grid axis pointer is NULL" in L.sr_last_error().decode()
+
+
+def test_config_set_get_clear_on_host_fields():
+    """sr_config_set pins a work shape for problems of these sizes,
+    sr_config_get returns it and sr_config_clear restores the default; bad
+    shapes and non-mixed precisions are refused (host fields only)."""
+    import ctypes
+    from synchrad_gb300 import _lib
+    L = _lib.lib()
+    t, g = _lib.SrTracks(), _lib.SrGrid()
+    t.n_tracks, t.total_steps, t.dtype = 3, 300, _lib.SR_DTYPE_F64
+    g.n_omega, g.n_theta, g.n_phi, g.dtype = 512, 4, 4, _lib.SR_DTYPE_F64
+    tp, gp = ctypes.byref(t), ctypes.byref(g)
+    L.sr_config_clear()
+    dflt = _lib.SrConfig()
+    assert L.sr_config_get(tp, gp, 0, 3, ctypes.byref(dflt)) == 0
+    pin = _lib.SrConfig(16, 8, 256, 2, 0, 0, 0.0)
+    assert L.sr_config_set(tp, gp, 0, 3, ctypes.byref(pin)) == 0
+    got = _lib.SrConfig()
+    assert L.sr_config_get(tp, gp, 0, 3, ctypes.byref(got)) == 0
+    assert (got.points_per_lane, got.lanes_per_direction, got.steps_per_stage,
+            got.track_subsets) == (16, 8, 256, 2)
+    other = _lib.SrConfig()
+    assert L.sr_config_get(tp, gp, 1, 3, ctypes.byref(other)) == 0   # another comp: default
+    assert other.as_dict() == dflt.as_dict()
+    assert L.sr_config_clear() == 0
+    assert L.sr_config_get(tp, gp, 0, 3, ctypes.byref(got)) == 0
+    assert got.as_dict() == dflt.as_dict()
+    for bad in ((12, 8, 256, 0), (16, 4, 256, 0), (16, 8, 48, 0), (16, 8, 1024, 0),
+                (16, 8, 256, 65)):
+        assert L.sr_config_set(tp, gp, 0, 3, ctypes.byref(_lib.SrConfig(*bad, 0, 0, 0.0))) \
+            == _lib.SR_ERR_INVALID, bad
+    assert L.sr_config_set(tp, gp, 0, _lib.SR_PREC_DOUBLE, ctypes.byref(pin)) == \
+        _lib.SR_ERR_UNSUPPORTED
