@@ -4,7 +4,11 @@
  * The library evaluates SynchRad's far-field (Lienard-Wiechert spectral sum
  * over track steps, per (omega, theta, phi) point) and near-field (screen at a
  * finite distance) integrals on the GPU.  All pointers named "device" are CUDA
- * device pointers owned by the caller; nothing here allocates device memory.
+ * device pointers owned by the caller.  Three diagnostics and tuning calls
+ * allocate: sr_autotune (device scratch and outputs for its trial runs, freed
+ * before it returns), sr_probe_fp32_peak (a 16-byte stream-ordered buffer) and
+ * sr_graph_create (a private stream and the graph objects); no other entry
+ * point allocates device memory.
  * Every entry point is stream-ordered on `stream` (a cudaStream_t, NULL for the
  * legacy default stream), returns SR_OK or a negative SR_ERR_* code, and leaves
  * a message for sr_last_error() on failure.  Output spectra are accumulated in
@@ -125,10 +129,20 @@ int sr_spectrum(const sr_tracks *tracks, const sr_grid *grid, int comp,
  * it until the process exits.  Sizes whose scratch (80 B per track step, 8 B
  * per point x output x snapshot, plus per-CTA sums) exceeds it are rejected
  * with SR_ERR_INVALID.  The first call on a device looks up the array's device
- * address (make it before any stream capture); calls that overlap on the GPU
- * share the array and race.  Far field only; outputs are double, accumulated. */
+ * address (make it before any stream capture); that address is kept for the
+ * process and does not survive cudaDeviceReset.  Calls that overlap on the GPU
+ * share the array and race.  Far field only; outputs are double, accumulated.
+ * A bounded kernel wait that ran out of time is reported by sr_noalloc_status,
+ * not by the return code. */
 int sr_spectrum_noalloc(const sr_tracks *tracks, const sr_grid *grid, int comp,
                         void *const *out, void *stream);
+
+/* Synchronises `stream` and reads the kernels' status word of the last
+ * sr_spectrum_noalloc call on the current device (it lives in the static
+ * array; the next call clears it): SR_OK, or SR_ERR_TIMEOUT if a bounded wait
+ * expired and that call's outputs are incomplete.  Allocates nothing.  No
+ * counterpart in the reference. */
+int sr_noalloc_status(void *stream);
 
 /* Scratch bytes sr_spectrum needs for these sizes (reads host fields only):
  * 0 for SR_PREC_DOUBLE and SR_PREC_FLOAT*, which need none; SR_ERR_INVALID
@@ -268,6 +282,8 @@ int sr_probe_fp32_peak(double *tflops_scalar, double *tflops_packed, void *strea
  * completes, with a limit of limit_ns (1 .. 1e9); the kernel records the
  * timeout in the status word at the start of `workspace` (>= 4 bytes) as the
  * spectrum kernels do, and sr_workspace_status then returns SR_ERR_TIMEOUT.
+ * With `workspace` NULL the target is the status word of sr_spectrum_noalloc's
+ * static array, read back by sr_noalloc_status.
  * No copy is issued and the context stays usable. */
 int sr_selftest_wait_timeout(int64_t limit_ns, void *workspace, void *stream);
 

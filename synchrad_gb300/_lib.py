@@ -106,7 +106,8 @@ EXPORTS = (
     "sr_far_cartesian_comps_complex", "sr_far_spheric_comps",
     "sr_far_spheric_comps_complex", "sr_near_total", "sr_near_cartesian_comps",
     "sr_near_cartesian_comps_complex", "sr_timing_enable", "sr_timing_read",
-    "sr_probe_fp32_peak", "sr_spectrum_noalloc", "sr_far_total_forward_saved",
+    "sr_probe_fp32_peak", "sr_spectrum_noalloc", "sr_noalloc_status",
+    "sr_far_total_forward_saved",
     "sr_far_total_backward_workspace_bytes", "sr_far_total_backward",
     "sr_autotune", "sr_config_get", "sr_config_set", "sr_config_clear", "sr_graph_create", "sr_graph_launch",
     "sr_graph_nodes", "sr_graph_destroy", "sr_near_total_forward_saved",
@@ -126,6 +127,8 @@ def _declare(L: ctypes.CDLL) -> None:
     L.sr_spectrum_noalloc.restype = i32
     L.sr_spectrum_noalloc.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid), i32,
                                       ctypes.POINTER(vp), vp]
+    L.sr_noalloc_status.restype = i32
+    L.sr_noalloc_status.argtypes = [vp]
     L.sr_far_total_forward_saved.restype = i32
     L.sr_far_total_forward_saved.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid),
                                              vp, vp, vp, ctypes.c_size_t, vp]

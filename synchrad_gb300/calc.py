@@ -357,7 +357,11 @@ class SynchRad(Utilities):
         self.Data["radiation"] = out
 
     def _gather_result_dist(self):
-        """Sum the ranks' spectra and weights on rank 0 (synchrad/calc.py:560-571)."""
+        """Sum the ranks' spectra and weights on rank 0 (synchrad/calc.py:560-571).
+
+        As there, only rank 0 holds the sums afterwards; the other ranks are
+        left with zero spectra and ``total_weight`` None (the receive buffers
+        of the reference's Reduce and the non-root result of its reduce)."""
         dist = self.comm
         # NCCL reduces device tensors only; gloo (and others) take host tensors
         on_dev = (str(dist.get_backend()).lower() == "nccl" and self.device is not None)
@@ -366,11 +370,12 @@ class SynchRad(Utilities):
             if on_dev:
                 t = t.to(self.device)
             dist.reduce(t, dst=0)
-            self.Data["radiation"][key] = t.cpu().numpy()
+            summed = t.cpu().numpy()
+            self.Data["radiation"][key] = summed if self.rank == 0 else np.zeros_like(summed)
         tw = torch.tensor([float(self.total_weight)], dtype=torch.float64,
                           device=self.device if on_dev else "cpu")
         dist.reduce(tw, dst=0)
-        self.total_weight = float(tw[0]) if self.rank == 0 else self.total_weight
+        self.total_weight = float(tw[0]) if self.rank == 0 else None
 
     def _read_args(self, file_spectrum):
         """synchrad/calc.py:648-666 (needs h5py)."""

@@ -173,9 +173,14 @@ __global__ void wait_timeout_selftest_kernel(int *status, uint64_t limit_ns) {
 
 extern "C" int sr_selftest_wait_timeout(int64_t limit_ns, void *workspace, void *stream) {
   clear_error();
-  if (!workspace) return fail(SR_ERR_INVALID, "workspace is NULL");
   if (limit_ns <= 0 || limit_ns > 1000000000ll)
     return fail(SR_ERR_INVALID, "limit %lld ns (1 .. 1e9)", (long long)limit_ns);
+  if (!workspace) {  // the static scratch of sr_spectrum_noalloc
+    int *word = nullptr;
+    const int rc = noalloc_status_word(&word);
+    if (rc) return rc;
+    workspace = word;
+  }
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e = cudaMemsetAsync(workspace, 0, sizeof(int), s);
   if (e != cudaSuccess) return cuda_fail(e, "status reset");

@@ -116,4 +116,8 @@ FarMixedParams make_far_mixed_params(const sr_tracks *t, const sr_grid *g,
                                      int comp, void *const *out);
 int device_sm_count();
 
+// sr_noalloc.cu: the status word of the allocation-free entry point's static
+// scratch array on the current device.
+int noalloc_status_word(int **word);
+
 }  // namespace sr

@@ -12,9 +12,17 @@
 // Host code cannot use the array's name as a device address: it names a
 // host-side stand-in.  The device address is looked up once per device, on the
 // first call made with that device current, by cudaGetSymbolAddress; that first
-// call should therefore come before any stream capture.  All calls share the
-// one array: calls that overlap on the GPU (two streams, or two host threads)
-// race, and each call clears what must start at zero.
+// call should therefore come before any stream capture.  The cached address
+// belongs to the device's context at that time: it does not survive
+// cudaDeviceReset (or a primary context released and created again), after
+// which these entry points must not be called in the same process.  All calls
+// share the one array: calls that overlap on the GPU (two streams, or two host
+// threads) race, and each call clears what must start at zero.
+//
+// The first 256 bytes of the array hold the kernels' status word, as at the
+// start of sr_spectrum's workspace.  sr_noalloc_status reads it back: a bounded
+// wait that ran out of time in the last call is reported there, not by the
+// call's return code (the call returns once its kernels are queued).
 #include <mutex>
 
 #include "sr_common.cuh"
@@ -49,9 +57,36 @@ int scratch_address(void **addr) {
 }
 
 }  // namespace
+
+// The status word at the start of the static array, on the current device
+// (sr_selftest_wait_timeout's target when it is given no workspace).
+int noalloc_status_word(int **word) {
+  void *p = nullptr;
+  const int rc = scratch_address(&p);
+  if (rc) return rc;
+  *word = (int *)p;
+  return SR_OK;
+}
+
 }  // namespace sr
 
 using namespace sr;
+
+extern "C" int sr_noalloc_status(void *stream) {
+  clear_error();
+  int *word = nullptr;
+  int rc = noalloc_status_word(&word);
+  if (rc) return rc;
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "stream synchronize");
+  int status = 0;
+  e = cudaMemcpy(&status, word, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "status read");
+  if (status == STATUS_WAIT_TIMEOUT)
+    return fail(SR_ERR_TIMEOUT, "a kernel wait on a staged copy ran out of time in the last "
+                                "sr_spectrum_noalloc call; its outputs are incomplete");
+  return SR_OK;
+}
 
 extern "C" int sr_spectrum_noalloc(const sr_tracks *t, const sr_grid *g, int comp,
                                    void *const *out, void *stream) {

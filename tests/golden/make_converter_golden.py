@@ -18,6 +18,7 @@ Run from the repository root, where the reference tree is available:
 from __future__ import annotations
 
 import ast
+import os
 import json
 import sys
 import types
@@ -26,7 +27,7 @@ from pathlib import Path
 
 import numpy as np
 
-REF = Path("/root/reference/synchrad/converters.py")
+REF = Path(os.environ.get("SR_REFERENCE_ROOT", "/root/reference")) / "synchrad" / "converters.py"
 TESTS = Path(__file__).resolve().parents[1]
 OUT = Path(__file__).resolve().parent / "converters_golden.npz"
 sys.path.insert(0, str(TESTS))

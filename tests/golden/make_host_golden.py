@@ -24,6 +24,7 @@ Run from the repository root, where the reference tree is available:
 from __future__ import annotations
 
 import ast
+import os
 import json
 import sys
 import types
@@ -31,7 +32,7 @@ from pathlib import Path
 
 import numpy as np
 
-REF = Path("/root/reference/synchrad")
+REF = Path(os.environ.get("SR_REFERENCE_ROOT", "/root/reference")) / "synchrad"
 OUT = Path(__file__).resolve().parent / "host_golden.npz"
 
 

@@ -15,13 +15,14 @@ golden spectra and to cross-check the oracle's host restatement.
 from __future__ import annotations
 
 import ast
+import os
 import sys
 import types
 from pathlib import Path
 
 import numpy as np
 
-REF = Path("/root/reference/synchrad")
+REF = Path(os.environ.get("SR_REFERENCE_ROOT", "/root/reference")) / "synchrad"
 ROOT = Path(__file__).resolve().parents[2]
 if str(ROOT) not in sys.path:
     sys.path.insert(0, str(ROOT))

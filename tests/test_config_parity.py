@@ -1,0 +1,94 @@
+"""Mixed precision against the CPU oracle at the benchmark configurations' own scale.
+
+The small golden cases pin every comp, dtype and edge case; these tests pin the
+regimes the benchmark workloads live in, where the mixed path's double-float
+phase, rotation chains, aliasing mask and compensated sums are stressed hardest:
+
+* far field, 1024 undulator electrons (gamma 400, K = 1, 4000 steps), to the
+  third harmonic (0.5-3.5 omega_1) and theta up to 2/gamma;
+* far field, 8192 FP32 betatron tracks of 500-20000 steps: positions reach
+  z ~ 300 with FP32 rounding, so the |dphase| < pi mask cuts through the omega
+  axis on most steps (the shortest and the longest tracks of the batch);
+* near field, 2048 helical electrons, 8000 steps, screen at 20 undulator
+  lengths (L = 1000).
+
+Each test builds the workload with its default seed, takes whole tracks, keeps
+the full omega axis and the theta (or R) and phi ranges of the configuration
+on fewer nodes (the last theta / R node included), and compares
+``SynchRad(dtype='mixed')`` with the FP64 oracle (the reference kernels'
+arithmetic in C, ``oracle.host.calculate_spectrum``).  Bar: relative L2
+<= 1e-5; the largest relative error over points above 1e-3 of the maximum is
+reported and bounded.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from synchrad_gb300 import workloads as wl  # noqa: E402
+
+TOL_L2 = 1e-5          # relative L2, mixed vs FP64 oracle
+TOL_MAXREL = 1e-3      # largest relative error over points above FLOOR x max
+FLOOR = 1e-3
+
+
+def _need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def _compare(w, idx, sub_nodes, label):
+    from oracle import host
+    from synchrad_gb300.calc import SynchRad
+    g = w.args["grid"]
+    grid = [g[0], g[1], g[2], (g[3][0],) + tuple(sub_nodes)]
+    mode = w.args.get("mode", "far")
+    tracks = [list(w.tracks[i]) for i in idx]
+    steps = [int(np.asarray(t[0]).size) for t in tracks]
+    ref, *_ = host.calculate_spectrum({"grid": grid, "dtype": "double", "mode": mode},
+                                      [list(t) for t in tracks], w.time_step,
+                                      L_screen=w.L_screen)
+    calc = SynchRad({"grid": grid, "dtype": "mixed", "mode": mode})
+    calc.calculate_spectrum([list(t) for t in tracks], timeStep=w.time_step,
+                            L_screen=w.L_screen, verbose=False)
+    got = calc.Data["radiation"]["total"]
+    exp = ref["total"]
+    assert got.shape == exp.shape
+    rel = float(np.linalg.norm(got - exp) / np.linalg.norm(exp))
+    big = np.abs(exp) > FLOOR * np.abs(exp).max()
+    maxrel = float(np.max(np.abs(got[big] - exp[big]) / np.abs(exp[big])))
+    print(f"{label}: tracks {idx} ({steps} steps), grid {grid[-1]}: relative L2 "
+          f"{rel:.2e}, max relative {maxrel:.2e} over {int(big.sum())} points above "
+          f"{FLOOR:g} of max")
+    assert rel <= TOL_L2, f"{label}: relative L2 {rel:.3e}"
+    assert maxrel <= TOL_MAXREL, f"{label}: max relative {maxrel:.3e}"
+    return rel, maxrel
+
+
+def test_far_undulator_1024e_third_harmonic():
+    """Far field, 512 omega over 0.5-3.5 omega_1, theta in [0, 2/gamma]."""
+    _need_gpu()
+    w = wl.c2_far_mixed()
+    assert all(len(t[0]) == 4000 for t in w.tracks)
+    _compare(w, [0, 1, 511, 1023], (8, 8), "far 1024e")
+
+
+def test_far_betatron_ragged_fp32_extremes():
+    """Far field, FP32 betatron tracks: the two shortest and two longest."""
+    _need_gpu()
+    w = wl.c3_betatron_ragged()
+    lengths = np.array([len(t[0]) for t in w.tracks])
+    order = np.argsort(lengths, kind="stable")
+    idx = [int(order[0]), int(order[1]), int(order[-2]), int(order[-1])]
+    assert w.tracks[idx[-1]][0].dtype == np.float32
+    assert lengths[idx[-1]] > 19000 and lengths[idx[0]] < 600
+    _compare(w, idx, (6, 6), "far ragged FP32")
+
+
+def test_near_helical_8000_steps_screen():
+    """Near field, screen at L = 1000 (20 undulator lengths), R up to 1.5 L/gamma."""
+    _need_gpu()
+    w = wl.c5_near_helical()
+    assert all(len(t[0]) == 8000 for t in w.tracks)
+    _compare(w, [0, 2047], (6, 6), "near helical")

@@ -6,7 +6,8 @@ the same over torch.distributed.  Here each rank's per-track evaluation is
 the oracle (the GPU kernels need a device), everything else is SynchRad's
 own code: track striding, weight accumulation, the device-to-host layout
 swap and the reduction on rank 0.  The result must equal the oracle's
-single-process spectrum of all tracks.
+single-process spectrum of all tracks; the other rank is left with zero
+spectra and ``total_weight`` None, as after the reference's MPI reduction.
 """
 import os
 import socket
@@ -70,6 +71,11 @@ def _worker(rank, world, port, out_dir):
         if rank == 0:
             np.save(os.path.join(out_dir, "total.npy"), calc.Data["radiation"]["total"])
             np.save(os.path.join(out_dir, "weight.npy"), np.array([calc.total_weight]))
+        else:  # as after the reference's Reduce: zero spectra, no total weight
+            spec = calc.Data["radiation"]["total"]
+            np.save(os.path.join(out_dir, f"rank{rank}.npy"),
+                    np.array([float(np.abs(spec).max()), spec.size,
+                              float(calc.total_weight is None)]))
     finally:
         dist.destroy_process_group()
 
@@ -94,3 +100,5 @@ def test_two_gloo_ranks_match_one_process(tmp_path):
     assert got.shape == exp.shape
     assert np.linalg.norm(got - exp) / np.linalg.norm(exp) < 1e-13
     assert weight == pytest.approx(total_weight, rel=1e-14)
+    peak, size, weight_none = np.load(tmp_path / "rank1.npy")
+    assert peak == 0.0 and size == exp.size and weight_none == 1.0
