@@ -689,10 +689,14 @@ def main():
     e2e = None
     if not args.no_e2e:
         n_e2e = args.e2e_steps or args.steps
-        calc = SynchRad({"grid": w.args["grid"], "dtype": "mixed", "mode": mode})
+        e2e_args = {"grid": w.args["grid"], "dtype": "mixed", "mode": mode}
+        if not args.no_tune and args.shape is None:
+            # the work shapes of the streamed chunks are tuned in the warm call
+            e2e_args["autotune"] = min(args.tune_budget_ms, 3000.0)
+        calc = SynchRad(e2e_args)
         host_tracks = [list(t) for t in w.tracks]
         calc.calculate_spectrum(host_tracks, timeStep=w.time_step, verbose=False,
-                                L_screen=w.L_screen)  # warm
+                                L_screen=w.L_screen)  # warm (and tune)
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
@@ -712,7 +716,9 @@ def main():
         # (the reference's scheme): the whole job is pt_steps per call
         e2e = {"value": pt_steps * n_e2e / el / 1e9, "unit": UNIT,
                "scaling": "strong" if ws > 1 else "single GPU",
-               "h2d_bytes_per_step": int(batch.h2d_bytes),
+               "h2d_bytes_per_step": int(calc._h2d_bytes),
+               "h2d": "tracks streamed in chunks on a copy stream, packed and copied "
+                      "while the previous chunk computes",
                "d2h_bytes_per_step": int(P * 8),
                "steps": n_e2e, "ms_per_step": el / n_e2e * 1e3,
                "api": "SynchRad.calculate_spectrum (numpy tracks in, numpy spectrum out)",

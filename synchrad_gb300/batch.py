@@ -59,27 +59,44 @@ class TrackBatch:
         return s
 
 
-def _to_device(arr: np.ndarray, device, pinned: bool) -> torch.Tensor:
-    t = torch.from_numpy(np.ascontiguousarray(arr))
-    if pinned and device.type == "cuda":
-        t = t.pin_memory()
-    return t.to(device, non_blocking=pinned)
+_ALIGN = 256  # every array of a packed batch starts on a 256-byte boundary
 
 
-def _u32_view(a: np.ndarray) -> np.ndarray:
-    return np.ascontiguousarray(a, dtype=np.uint32).view(np.int32)
+def _round_up(n: int) -> int:
+    return (n + _ALIGN - 1) // _ALIGN * _ALIGN
 
 
-def pack_tracks(tracks, np_dtype, n_snaps, dt, it_range=None, device=None,
-                pinned=True) -> TrackBatch:
-    """Pack reference-format tracks ``[x, y, z, ux, uy, uz, w(, it_start)]``.
+@dataclass
+class _Packing:
+    """Host-side description of a batch: per-track scalars and the byte
+    layout of its single contiguous buffer (CSR offsets, x..uz, weight,
+    it_start, it_end, snapshot rows, in that order)."""
+    lengths: np.ndarray
+    offsets: np.ndarray
+    weight: np.ndarray
+    it_start: np.ndarray
+    it_end: np.ndarray
+    snaps: np.ndarray
+    stride: int
+    itemsize: int
+    starts: list
+    nbytes: int
 
-    Per-track launch scalars follow ``synchrad/calc.py:292-301, 306-307``:
+    @property
+    def total(self) -> int:
+        return int(self.offsets[-1])
+
+    @property
+    def payload_bytes(self) -> int:
+        return int(self.offsets.nbytes + 6 * self.total * self.itemsize + self.weight.nbytes
+                   + self.it_start.nbytes + self.it_end.nbytes + self.snaps.nbytes)
+
+
+def _plan(tracks, np_dtype, n_snaps, it_range) -> _Packing:
+    """Per-track launch scalars of ``synchrad/calc.py:292-301, 306-307``:
     without ``it_range`` every track starts at 0 with itEnd = its length and its
     own snapshot row; with ``it_range`` the track's ``it_start`` is kept and
-    every track shares one snapshot row and itEnd = it_range[-1].
-    """
-    device = torch.device(device) if device is not None else torch.device("cuda")
+    every track shares one snapshot row and itEnd = it_range[-1]."""
     n = len(tracks)
     lengths = np.array([np.asarray(t[0]).size for t in tracks], dtype=np.int64)
     for i, t in enumerate(tracks):
@@ -91,13 +108,6 @@ def pack_tracks(tracks, np_dtype, n_snaps, dt, it_range=None, device=None,
                          "(the reference's unsigned loop bounds would wrap)")
     offsets = np.zeros(n + 1, dtype=np.int64)
     np.cumsum(lengths, out=offsets[1:])
-    total = int(offsets[-1])
-    coords = []
-    for k in range(6):
-        buf = np.empty(total, dtype=np_dtype)
-        for i, t in enumerate(tracks):
-            buf[offsets[i]:offsets[i + 1]] = np.asarray(t[k])
-        coords.append(buf)
     weight = np.array([float(t[6]) for t in tracks], dtype=np.float64)
     if it_range is None:
         it_start = np.zeros(n, dtype=np.uint32)
@@ -115,12 +125,132 @@ def pack_tracks(tracks, np_dtype, n_snaps, dt, it_range=None, device=None,
         stride = 0
     if n_snaps and snaps.size == 0:
         snaps = np.zeros(max(int(n_snaps), 1), np.uint32)
-    host = [offsets, *coords, weight, _u32_view(it_start), _u32_view(it_end), _u32_view(snaps)]
-    dev = [_to_device(a, device, pinned) for a in host]
-    h2d = int(sum(a.nbytes for a in host))
-    return TrackBatch(n, torch.float32 if np_dtype == np.float32 else torch.float64, total,
-                      dev[0], dev[1:7], dev[7], dev[8], dev[9], dev[10], stride,
-                      int(n_snaps), float(dt), h2d)
+    itemsize = np.dtype(np_dtype).itemsize
+    total = int(offsets[-1])
+    sizes = [offsets.nbytes] + [total * itemsize] * 6 + [weight.nbytes, 4 * n, 4 * n,
+                                                        4 * snaps.size]
+    starts, pos = [], 0
+    for sz in sizes:
+        starts.append(pos)
+        pos += _round_up(sz)
+    return _Packing(lengths, offsets, weight, it_start, it_end,
+                    np.ascontiguousarray(snaps, dtype=np.uint32), stride, itemsize, starts,
+                    max(pos, _ALIGN))
+
+
+def _fill(buf: np.ndarray, pk: _Packing, tracks, np_dtype) -> None:
+    """Write the batch into the uint8 host buffer ``buf`` (pk.nbytes long)."""
+    def view(i, dtype, count):
+        return buf[pk.starts[i]:pk.starts[i] + count * np.dtype(dtype).itemsize].view(dtype)
+
+    n, total = len(tracks), pk.total
+    view(0, np.int64, n + 1)[:] = pk.offsets
+    for k in range(6):
+        dst = view(1 + k, np_dtype, total)
+        for i, t in enumerate(tracks):
+            dst[pk.offsets[i]:pk.offsets[i + 1]] = np.asarray(t[k])
+    view(7, np.float64, n)[:] = pk.weight
+    view(8, np.uint32, n)[:] = pk.it_start
+    view(9, np.uint32, n)[:] = pk.it_end
+    view(10, np.uint32, pk.snaps.size)[:] = pk.snaps
+
+
+def _batch_on(dev: torch.Tensor, pk: _Packing, np_dtype, n_snaps, dt) -> TrackBatch:
+    """TrackBatch whose arrays are views of the device buffer ``dev``."""
+    tdt = torch.float32 if np_dtype == np.float32 else torch.float64
+    n, total = len(pk.weight), pk.total
+
+    def view(i, dtype, count, nbytes):
+        return dev[pk.starts[i]:pk.starts[i] + count * nbytes].view(dtype)
+
+    coords = [view(1 + k, tdt, total, pk.itemsize) for k in range(6)]
+    return TrackBatch(n, tdt, total, view(0, torch.int64, n + 1, 8), coords,
+                      view(7, torch.float64, n, 8), view(8, torch.int32, n, 4),
+                      view(9, torch.int32, n, 4), view(10, torch.int32, pk.snaps.size, 4),
+                      pk.stride, int(n_snaps), float(dt), pk.payload_bytes)
+
+
+def pack_tracks(tracks, np_dtype, n_snaps, dt, it_range=None, device=None,
+                pinned=True) -> TrackBatch:
+    """Pack reference-format tracks ``[x, y, z, ux, uy, uz, w(, it_start)]``
+    into one contiguous (pinned) host buffer and copy it to the device at once.
+
+    Per-track launch scalars follow ``synchrad/calc.py:292-301, 306-307``
+    (see ``_plan``)."""
+    device = torch.device(device) if device is not None else torch.device("cuda")
+    pk = _plan(tracks, np_dtype, n_snaps, it_range)
+    pin = pinned and device.type == "cuda"
+    host = torch.empty(pk.nbytes, dtype=torch.uint8, pin_memory=pin)
+    _fill(host.numpy(), pk, tracks, np_dtype)
+    dev = host.to(device, non_blocking=pin)
+    return _batch_on(dev, pk, np_dtype, n_snaps, dt)
+
+
+def plan_chunks(lengths, itemsize: int, min_bytes: int = 32 << 20, n_chunks: int = 8,
+                lead_fraction: float = 1.0 / 32) -> list:
+    """Track ranges [t0, t1) for streaming a batch to the device in pieces.
+
+    Batches under ``min_bytes`` of coordinates stay whole.  Otherwise a small
+    leading chunk (about ``lead_fraction`` of the steps: the only upload not
+    hidden behind compute) is followed by about ``n_chunks`` chunks of equal
+    step counts; chunks hold whole tracks."""
+    lengths = np.asarray(lengths, dtype=np.int64)
+    n = lengths.size
+    total = int(lengths.sum())
+    if n <= 1 or 6 * total * itemsize < min_bytes:
+        return [(0, n)]
+    cum = np.cumsum(lengths)
+    cuts = [0]
+    lead = max(1, int(np.searchsorted(cum, lead_fraction * total, side="left")) + 1)
+    if lead < n:
+        cuts.append(lead)
+    rest0 = int(cum[cuts[-1] - 1])
+    step = (total - rest0) / n_chunks
+    for k in range(1, n_chunks):
+        t = int(np.searchsorted(cum, rest0 + k * step, side="left")) + 1
+        if cuts[-1] < t < n:
+            cuts.append(t)
+    cuts.append(n)
+    return list(zip(cuts[:-1], cuts[1:]))
+
+
+class TrackStream:
+    """Streams a batch to the device chunk by chunk so that the host packing
+    and the host-to-device copy of chunk k+1 run while chunk k is evaluated.
+
+    Each chunk is packed into a pinned host buffer, copied on a private copy
+    stream into a device buffer allocated on that stream (and marked as used
+    by the compute stream), and the compute stream waits for the copy's event
+    before the chunk's ``sr_spectrum`` call.  Chunks accumulate into the same
+    outputs, as the reference's one launch per track does
+    (``synchrad/calc.py:257-267``); for a fixed chunking the result is
+    deterministic."""
+
+    def __init__(self, device):
+        self.device = torch.device(device)
+        self.copy_stream = torch.cuda.Stream(self.device)
+
+    def chunks(self, tracks, np_dtype, n_snaps, dt, it_range=None, compute_stream=None,
+               plan=None):
+        """Yields (TrackBatch, first track index) per chunk; the batch's arrays
+        are ready for work queued on ``compute_stream`` after the yield."""
+        cur = compute_stream or torch.cuda.current_stream(self.device)
+        lengths = [np.asarray(t[0]).size for t in tracks]
+        if plan is None:
+            plan = plan_chunks(lengths, np.dtype(np_dtype).itemsize)
+        for t0, t1 in plan:
+            part = tracks[t0:t1]
+            pk = _plan(part, np_dtype, n_snaps, it_range)
+            host = torch.empty(pk.nbytes, dtype=torch.uint8, pin_memory=True)
+            _fill(host.numpy(), pk, part, np_dtype)
+            with torch.cuda.stream(self.copy_stream):
+                dev = torch.empty(pk.nbytes, dtype=torch.uint8, device=self.device)
+                dev.copy_(host, non_blocking=True)
+                ready = torch.cuda.Event()
+                ready.record(self.copy_stream)
+            dev.record_stream(cur)
+            cur.wait_event(ready)
+            yield _batch_on(dev, pk, np_dtype, n_snaps, dt), t0
 
 
 @dataclass

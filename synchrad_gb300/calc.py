@@ -26,8 +26,8 @@ import numpy as np
 import torch
 
 from . import _lib
-from .batch import (Workspace, autotune, make_grid, pack_tracks, precision_id, run_spectrum,
-                    snap_iterations)
+from .batch import (TrackStream, Workspace, autotune, make_grid, pack_tracks, precision_id,
+                    run_spectrum, snap_iterations)
 from .utils import Utilities
 
 VEC_COMPS = {
@@ -146,23 +146,46 @@ class SynchRad(Utilities):
         else:  # mixed: FP32 tracks stay FP32 (C3-style inputs), others FP64
             all32 = all(np.asarray(t[k]).dtype == np.float32 for t in tracks for k in range(6))
             np_dtype = np.float32 if all32 else np.float64
-        batch = pack_tracks(tracks, np_dtype, int(nSnaps), float(dt), it_range=it_range,
-                            device=self.device)
         if it_range is None:
             last = int(np.asarray(tracks[-1][0]).size)
             self.snap_iterations = snap_iterations((0, last), nSnaps)
         outs = [self._spect_dev[k] for k in VEC_COMPS[comp]]
         prec = precision_id(name, "native" in self.Args)
         tune = self.Args.get("autotune")  # not a reference key: True or a budget in ms
-        if tune and name == "mixed":
-            key = (batch.n_tracks, batch.total_steps, comp, int(nSnaps))
-            done = self.__dict__.setdefault("_tuned", set())
-            if key not in done:
-                budget = 3000.0 if tune is True else float(tune)
-                autotune(batch, self._grid_dev, comp, prec, budget)
-                done.add(key)
-        run_spectrum(batch, self._grid_dev, comp, prec, outs,
-                     workspace=self._workspace, check_status=True)
+        done = self.__dict__.setdefault("_tuned", set())
+        sticky = torch.zeros(1, dtype=torch.int32, device=self.device)
+        if self.device.type == "cuda":
+            if getattr(self, "_stream", None) is None:
+                self._stream = TrackStream(self.device)
+            compute = torch.cuda.current_stream(self.device)
+            # Chunks are packed and copied while the previous chunk is
+            # evaluated; each call's kernel status word is or-ed into one flag
+            # on the device, read once at the end (a read per chunk would
+            # serialise the stream).
+            batches = self._stream.chunks(tracks, np_dtype, int(nSnaps), float(dt),
+                                          it_range=it_range, compute_stream=compute)
+        else:  # host-placed arrays (checks of the host logic without a device)
+            compute = None
+            batches = [(pack_tracks(tracks, np_dtype, int(nSnaps), float(dt), it_range=it_range,
+                                    device=self.device), 0)]
+        self._h2d_bytes = 0
+        for batch, _ in batches:
+            self._h2d_bytes += batch.h2d_bytes
+            if tune and name == "mixed":
+                key = (batch.n_tracks, batch.total_steps, comp, int(nSnaps))
+                if key not in done:
+                    budget = 3000.0 if tune is True else float(tune)
+                    autotune(batch, self._grid_dev, comp, prec, budget, stream=compute)
+                    done.add(key)
+            run_spectrum(batch, self._grid_dev, comp, prec, outs,
+                         workspace=self._workspace, stream=compute)
+            ws = self._workspace.buf
+            if prec == _lib.SR_PREC_MIXED and ws is not None:
+                sticky.bitwise_or_(ws[:4].view(torch.int32))
+        if int(sticky.item()) != 0:
+            raise _lib.SynchRadError(_lib.SR_ERR_TIMEOUT,
+                                     "a kernel wait on a staged copy ran out of time; the "
+                                     "spectrum is incomplete")
 
     def _read_tracks(self, file_tracks, it_range, nSnaps, Np_max, verbose):
         """synchrad/calc.py:186-219 (needs h5py)."""

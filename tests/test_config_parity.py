@@ -29,7 +29,7 @@ pytestmark = pytest.mark.gpu
 from synchrad_gb300 import workloads as wl  # noqa: E402
 
 TOL_L2 = 1e-5          # relative L2, mixed vs FP64 oracle
-TOL_MAXREL = 1e-3      # largest relative error over points above FLOOR x max
+TOL_MAXREL = 1e-4      # largest relative error over points above FLOOR x max (measured <= 3e-5)
 FLOOR = 1e-3
 
 
