@@ -112,8 +112,10 @@ def _plan(tracks, np_dtype, n_snaps, it_range) -> _Packing:
     if it_range is None:
         it_start = np.zeros(n, dtype=np.uint32)
         it_end = lengths.astype(np.uint32)
-        rows = [snap_iterations((0, int(L)), n_snaps) for L in lengths]
-        snaps = np.concatenate(rows) if rows else np.zeros(0, np.uint32)
+        # every track's own row, snap_iterations((0, length), n_snaps), at once
+        rows = np.linspace(np.zeros(n), lengths.astype(np.float64), int(n_snaps) + 1, axis=1,
+                           dtype=np.uint32)[:, 1:]
+        snaps = np.ascontiguousarray(rows).ravel()
         stride = int(n_snaps)
     else:
         it_start = np.array([int(t[7]) if len(t) == 8 else 0 for t in tracks], dtype=np.uint32)
@@ -146,9 +148,9 @@ def _fill(buf: np.ndarray, pk: _Packing, tracks, np_dtype) -> None:
     n, total = len(tracks), pk.total
     view(0, np.int64, n + 1)[:] = pk.offsets
     for k in range(6):
-        dst = view(1 + k, np_dtype, total)
-        for i, t in enumerate(tracks):
-            dst[pk.offsets[i]:pk.offsets[i + 1]] = np.asarray(t[k])
+        if n:
+            np.concatenate([np.asarray(t[k]).ravel() for t in tracks],
+                           out=view(1 + k, np_dtype, total))
     view(7, np.float64, n)[:] = pk.weight
     view(8, np.uint32, n)[:] = pk.it_start
     view(9, np.uint32, n)[:] = pk.it_end
@@ -220,25 +222,30 @@ class TrackStream:
 
     Each chunk is packed into a pinned host buffer, copied on a private copy
     stream into a device buffer allocated on that stream (and marked as used
-    by the compute stream), and the compute stream waits for the copy's event
-    before the chunk's ``sr_spectrum`` call.  Chunks accumulate into the same
-    outputs, as the reference's one launch per track does
-    (``synchrad/calc.py:257-267``); for a fixed chunking the result is
-    deterministic."""
+    by the chunk's compute stream), and the compute stream waits for the
+    copy's event before the chunk's ``sr_spectrum`` call.  With two compute
+    streams, consecutive chunks' persistent launches overlap: the next chunk's
+    CTAs take the SMs the previous chunk's last work items free.  The
+    reference launches one kernel per track (``synchrad/calc.py:257-267``);
+    for a fixed chunking the result here is deterministic."""
 
     def __init__(self, device):
         self.device = torch.device(device)
         self.copy_stream = torch.cuda.Stream(self.device)
 
     def chunks(self, tracks, np_dtype, n_snaps, dt, it_range=None, compute_stream=None,
-               plan=None):
-        """Yields (TrackBatch, first track index) per chunk; the batch's arrays
-        are ready for work queued on ``compute_stream`` after the yield."""
-        cur = compute_stream or torch.cuda.current_stream(self.device)
+               plan=None, compute_streams=None):
+        """Yields (TrackBatch, first track index, stream) per chunk; the batch's
+        arrays are ready for work queued on that stream after the yield.
+        Chunk i goes to ``compute_streams[i % len(compute_streams)]`` (default:
+        ``compute_stream``, else the current stream)."""
+        if compute_streams is None:
+            compute_streams = [compute_stream or torch.cuda.current_stream(self.device)]
         lengths = [np.asarray(t[0]).size for t in tracks]
         if plan is None:
             plan = plan_chunks(lengths, np.dtype(np_dtype).itemsize)
-        for t0, t1 in plan:
+        for i, (t0, t1) in enumerate(plan):
+            cur = compute_streams[i % len(compute_streams)]
             part = tracks[t0:t1]
             pk = _plan(part, np_dtype, n_snaps, it_range)
             host = torch.empty(pk.nbytes, dtype=torch.uint8, pin_memory=True)
@@ -250,7 +257,7 @@ class TrackStream:
                 ready.record(self.copy_stream)
             dev.record_stream(cur)
             cur.wait_event(ready)
-            yield _batch_on(dev, pk, np_dtype, n_snaps, dt), t0
+            yield _batch_on(dev, pk, np_dtype, n_snaps, dt), t0, cur
 
 
 @dataclass

@@ -26,8 +26,8 @@ import numpy as np
 import torch
 
 from . import _lib
-from .batch import (TrackStream, Workspace, autotune, make_grid, pack_tracks, precision_id,
-                    run_spectrum, snap_iterations)
+from .batch import (TrackStream, Workspace, autotune, make_grid, pack_tracks, plan_chunks,
+                    precision_id, run_spectrum, snap_iterations)
 from .utils import Utilities
 
 VEC_COMPS = {
@@ -153,36 +153,62 @@ class SynchRad(Utilities):
         prec = precision_id(name, "native" in self.Args)
         tune = self.Args.get("autotune")  # not a reference key: True or a budget in ms
         done = self.__dict__.setdefault("_tuned", set())
-        sticky = torch.zeros(1, dtype=torch.int32, device=self.device)
-        if self.device.type == "cuda":
-            if getattr(self, "_stream", None) is None:
-                self._stream = TrackStream(self.device)
-            compute = torch.cuda.current_stream(self.device)
-            # Chunks are packed and copied while the previous chunk is
-            # evaluated; each call's kernel status word is or-ed into one flag
-            # on the device, read once at the end (a read per chunk would
-            # serialise the stream).
-            batches = self._stream.chunks(tracks, np_dtype, int(nSnaps), float(dt),
-                                          it_range=it_range, compute_stream=compute)
-        else:  # host-placed arrays (checks of the host logic without a device)
-            compute = None
-            batches = [(pack_tracks(tracks, np_dtype, int(nSnaps), float(dt), it_range=it_range,
-                                    device=self.device), 0)]
+        if self.device.type != "cuda":  # host-placed arrays (checks of the host logic)
+            batch = pack_tracks(tracks, np_dtype, int(nSnaps), float(dt), it_range=it_range,
+                                device=self.device)
+            self._h2d_bytes = batch.h2d_bytes
+            run_spectrum(batch, self._grid_dev, comp, prec, outs, workspace=self._workspace)
+            return
+        cur = torch.cuda.current_stream(self.device)
+        if getattr(self, "_stream", None) is None:
+            self._stream = TrackStream(self.device)
+            self._lanes = ((torch.cuda.Stream(self.device), self._workspace),
+                           (torch.cuda.Stream(self.device), Workspace(self.device)))
+        plan = plan_chunks([np.asarray(t[0]).size for t in tracks], np.dtype(np_dtype).itemsize)
+        # One chunk: everything on the current stream.  Several: chunks
+        # alternate between two compute streams, each with its own workspace
+        # and accumulator (the second one added in at the end), so that a
+        # chunk's launch fills the SMs its predecessor's tail frees; the host
+        # packs and copies the next chunk meanwhile.
+        if len(plan) == 1:
+            lanes = [(cur, self._workspace, outs)]
+        else:
+            extra = [torch.zeros_like(o) for o in outs]
+            lanes = [(self._lanes[0][0], self._lanes[0][1], outs),
+                     (self._lanes[1][0], self._lanes[1][1], extra)]
+            for s_, _, o_ in lanes:
+                s_.wait_stream(cur)  # outputs zeroed on the current stream
+                for t_ in o_:
+                    t_.record_stream(s_)
+        # each call's kernel status word is or-ed into a flag per lane, read
+        # once at the end (a read per chunk would serialise the streams)
+        sticky = torch.zeros(len(lanes), dtype=torch.int32, device=self.device)
         self._h2d_bytes = 0
-        for batch, _ in batches:
+        chunks = self._stream.chunks(tracks, np_dtype, int(nSnaps), float(dt), it_range=it_range,
+                                     plan=plan, compute_streams=[ln[0] for ln in lanes])
+        for i, (batch, _, stream) in enumerate(chunks):
+            _, wsp, o_ = lanes[i % len(lanes)]
             self._h2d_bytes += batch.h2d_bytes
-            if tune and name == "mixed":
-                key = (batch.n_tracks, batch.total_steps, comp, int(nSnaps))
-                if key not in done:
-                    budget = 3000.0 if tune is True else float(tune)
-                    autotune(batch, self._grid_dev, comp, prec, budget, stream=compute)
-                    done.add(key)
-            run_spectrum(batch, self._grid_dev, comp, prec, outs,
-                         workspace=self._workspace, stream=compute)
-            ws = self._workspace.buf
-            if prec == _lib.SR_PREC_MIXED and ws is not None:
-                sticky.bitwise_or_(ws[:4].view(torch.int32))
-        if int(sticky.item()) != 0:
+            with torch.cuda.stream(stream):
+                if tune and name == "mixed":
+                    key = (batch.n_tracks, batch.total_steps, comp, int(nSnaps))
+                    if key not in done:
+                        budget = 3000.0 if tune is True else float(tune)
+                        autotune(batch, self._grid_dev, comp, prec, budget, stream=stream)
+                        done.add(key)
+                run_spectrum(batch, self._grid_dev, comp, prec, o_, workspace=wsp, stream=stream)
+                if wsp.buf is not None:
+                    # the buffer may have been allocated on another stream: its
+                    # memory is not handed out again before this stream's work
+                    wsp.buf.record_stream(stream)
+                    if prec == _lib.SR_PREC_MIXED:
+                        sticky[i % len(lanes)].bitwise_or_(wsp.buf[:4].view(torch.int32)[0])
+        if len(lanes) > 1:
+            for s_, _, _ in lanes:
+                cur.wait_stream(s_)
+            for o, e in zip(outs, lanes[1][2]):
+                o += e
+        if int(sticky.max().item()) != 0:
             raise _lib.SynchRadError(_lib.SR_ERR_TIMEOUT,
                                      "a kernel wait on a staged copy ran out of time; the "
                                      "spectrum is incomplete")
@@ -372,11 +398,13 @@ class SynchRad(Utilities):
                                    L_screen=self.dtype(L) if L is not None else 0.0)
 
     def _spectr_from_device(self, nSnaps):
-        """synchrad/calc.py:573-577: to host, (nSnaps, nOmega, nTheta, nPhi) float64."""
+        """synchrad/calc.py:573-577: to host, (nSnaps, nOmega, nTheta, nPhi)
+        float64; the axis swap and the widening of FP32 spectra are done on
+        the device (both exact), before the copy."""
         out = {}
         for key, t in self._spect_dev.items():
-            buff = t.cpu().numpy().swapaxes(-1, -3)
-            out[key] = np.ascontiguousarray(buff, dtype=np.double)
+            host = t.transpose(-1, -3).to(torch.float64).contiguous().cpu()
+            out[key] = host.numpy()
         self.Data["radiation"] = out
 
     def _gather_result_dist(self):

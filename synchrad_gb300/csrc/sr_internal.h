@@ -87,7 +87,7 @@ struct FarMixedConfig {
 FarMixedConfig far_mixed_make(uint32_t n_omega, uint32_t n_dirs, uint32_t n_tracks, int n_sm,
                               int K, int L, int stage, int n_sub);
 FarMixedConfig near_mixed_make(uint32_t n_omega, uint32_t n_screen, uint32_t n_tracks, int n_sm,
-                               int L, int n_sub);
+                               int K, int L, int n_sub);
 // The configuration sr_spectrum uses for a mixed-precision problem: the
 // autotuner's choice when one is cached for this problem, else the default.
 FarMixedConfig mixed_config(const sr_tracks *t, const sr_grid *g, int comp);

@@ -16,7 +16,8 @@
 //    rho^2 = (X - x)^2 + (Y - y)^2, with (t - z), x, y, z prepared in FP64;
 //    beta_z - n_z = (1 - n_z) - (1 - beta_z), 1 - n_z = rho^2/((r + L - z) r);
 //  * phasors, mask, compensated sums and FP64 results as in the far field
-//    (sr_far_mixed.cu), with K = 8 points per lane.
+//    (sr_far_mixed.cu), with K = 8 or 16 points per lane (six complex sums per
+//    point: 48 or 96 packed accumulator registers per lane).
 #include <algorithm>
 #include <cmath>
 
@@ -27,7 +28,7 @@
 namespace sr {
 namespace {
 
-constexpr int kNK = 8;          // points per lane
+constexpr int kNKDefault = 16;  // points per lane (8 or 16)
 constexpr int kNW = 8;          // warps per CTA
 constexpr int kNMaxDpw = 4;     // screen points per warp
 constexpr int kNOuter = 24;     // compensated values per point: 12 sums x (sum, comp)
@@ -96,13 +97,15 @@ struct NearSmemFixed {
 };
 
 // Packed accumulators of one lane: six complex sums for K points.
+template <int K>
 struct NearAcc {
-  float2 s1r[3][kNK / 2], s1i[3][kNK / 2];  // sum (beta - n)/r e^{i phi}, x y z
-  float2 s2r[3][kNK / 2], s2i[3][kNK / 2];  // sum n/r^2 e^{i phi}
+  float2 s1r[3][K / 2], s1i[3][K / 2];  // sum (beta - n)/r e^{i phi}, x y z
+  float2 s2r[3][K / 2], s2i[3][K / 2];  // sum n/r^2 e^{i phi}
 };
 
 // acc += amplitude (pairs) * Z for pair q.
-__device__ __forceinline__ void near_accumulate(NearAcc &a, int q, float2 zr, float2 zi,
+template <int K>
+__device__ __forceinline__ void near_accumulate(NearAcc<K> &a, int q, float2 zr, float2 zi,
                                                 const float2 (&bb)[3], const float2 (&aa)[3]) {
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
@@ -113,9 +116,10 @@ __device__ __forceinline__ void near_accumulate(NearAcc &a, int q, float2 zr, fl
   }
 }
 
-template <int W>
+template <int K, int W>
 __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p) {
-  constexpr int K = kNK, KP = K / 2, HP = KP / 2;
+  static_assert(K == 8 || K == 16, "K");
+  constexpr int KP = K / 2, HP = KP / 2;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   NearSmemFixed<W> &sm = *reinterpret_cast<NearSmemFixed<W> *>(smem_raw);
   const int dpw = (int)p.dpw, L = 32 / dpw;
@@ -200,7 +204,7 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
       SnapState snap;
       snap.init(it_start, it_end, snaps, p.n_snaps);
 
-      NearAcc acc;
+      NearAcc<K> acc;
 #pragma unroll
       for (int c = 0; c < 3; ++c)
 #pragma unroll
@@ -392,8 +396,9 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
                 sincosf(reduce_2pi(rp.hi, rp.lo), &Rs, &Rc);
                 float R2c, R2s;
                 cmul(Rc, Rs, Rc, Rs, R2c, R2s);
-                float Hc, Hs;
-                cmul(R2c, R2s, R2c, R2s, Hc, Hs);  // R^4 = R^(K/2)
+                float Hc = R2c, Hs = R2s;  // R^(K/2) by squaring R^2
+#pragma unroll
+                for (int e = K / 4; e > 1; e >>= 1) cmul(Hc, Hs, Hc, Hs, Hc, Hs);
                 // setup[dd][k][step]: consecutive lanes store consecutive float4
                 float4 *st = setup + (size_t)dd * kNSetupF4 * 32 + lane;
                 st[0 * 32] = make_float4(tau.hi, tau.lo, Rc, Rs);
@@ -553,16 +558,27 @@ size_t near_smem_bytes(int dpw) {
   return sizeof(NearSmemFixed<kNW>) + (size_t)kNW * 32 * dpw * kNSetupF4 * sizeof(float4);
 }
 
+template <int K>
+int launch_near_main(const FarMixedParams &p, int grid, cudaStream_t s) {
+  const size_t smem = near_smem_bytes((int)p.dpw);
+  cudaError_t e = cudaFuncSetAttribute(near_mixed_kernel<K, kNW>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return cuda_fail(e, "near_mixed smem attribute");
+  near_mixed_kernel<K, kNW><<<grid, kNW * 32, smem, s>>>(p);
+  return cuda_fail(cudaGetLastError(), "near_mixed kernel launch");
+}
+
 }  // namespace
 
-// A complete configuration from L lanes per direction and the track subsets
-// (0: enough subsets for about 16 work items per SM); K is fixed.
+// A complete configuration from K points per lane (8 or 16), L lanes per
+// direction and the track subsets (0: enough subsets for about 16 work items
+// per SM).
 FarMixedConfig near_mixed_make(uint32_t n_omega, uint32_t n_screen, uint32_t n_tracks, int n_sm,
-                               int L, int n_sub) {
+                               int K, int L, int n_sub) {
   FarMixedConfig c;
   c.W = kNW;
   c.ctas_per_sm = 1;
-  c.K = kNK;
+  c.K = K;
   c.stage = kStage;
   c.L = L;
   c.dpw = 32 / L;
@@ -581,11 +597,16 @@ FarMixedConfig near_mixed_make(uint32_t n_omega, uint32_t n_screen, uint32_t n_t
   return c;
 }
 
+// Default work shape: 16 points per lane (the per-step reseed and setup loads
+// amortised over twice the points of K = 8) wherever the omega axis fills
+// most of the lanes; short axes fall back to 8.
 FarMixedConfig near_mixed_choose(uint32_t n_omega, uint32_t n_screen, uint32_t n_tracks,
                                  int n_sm) {
+  int K = kNKDefault;
+  if ((uint32_t)(K * (32 / kNMaxDpw)) > n_omega + n_omega / 3) K = 8;
   int L = 32;
-  while (L > 32 / kNMaxDpw && (uint32_t)(L / 2) * kNK >= n_omega) L /= 2;
-  return near_mixed_make(n_omega, n_screen, n_tracks, n_sm, L, 0);
+  while (L > 32 / kNMaxDpw && (uint32_t)(L / 2) * K >= n_omega) L /= 2;
+  return near_mixed_make(n_omega, n_screen, n_tracks, n_sm, K, L, 0);
 }
 
 // The near-field step records for another kernel of the library (the adjoint).
@@ -647,15 +668,13 @@ int launch_near_mixed(FarMixedParams p, const FarMixedConfig &cfg, void *ws, siz
     int rc = cuda_fail(cudaGetLastError(), "near prepass launch");
     if (rc) return rc;
   }
-  const size_t smem = near_smem_bytes(cfg.dpw);
-  e = cudaFuncSetAttribute(near_mixed_kernel<kNW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem);
-  if (e != cudaSuccess) return cuda_fail(e, "near_mixed smem attribute");
+  if (cfg.K != 8 && cfg.K != 16)
+    return fail(SR_ERR_INVALID, "near field: points per lane %d (8 or 16)", cfg.K);
   void *tok = nullptr;
   timing_record(stream, true, &tok);
-  near_mixed_kernel<kNW><<<cfg.grid, kNW * 32, smem, stream>>>(p);
+  int rc = (cfg.K == 16) ? launch_near_main<16>(p, cfg.grid, stream)
+                         : launch_near_main<8>(p, cfg.grid, stream);
   timing_record(stream, false, &tok);
-  int rc = cuda_fail(cudaGetLastError(), "near_mixed kernel launch");
   if (rc) return rc;
   const uint64_t total = (uint64_t)p.n_out * p.n_snaps * P;
   uint64_t nb = (total + 255) / 256;

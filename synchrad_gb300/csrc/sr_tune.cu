@@ -4,7 +4,7 @@
 //
 // The free parameters of the persistent far-field launch are the points per
 // lane K, the lanes per direction L, the step records per TMA stage and the
-// number of track subsets (the near field: L and the subsets).  sr_autotune
+// number of track subsets (the near field: K, L and the subsets).  sr_autotune
 // times candidates with CUDA events on a bounded sample of the problem (the
 // leading tracks), by coordinate search: (K, L) first, then the stage size,
 // then the subsets, and caches the fastest per problem shape; sr_spectrum and
@@ -147,8 +147,8 @@ extern "C" int sr_config_set(const sr_tracks *t, const sr_grid *g, int comp, int
     return fail(SR_ERR_UNSUPPORTED, "only the mixed-precision kernels have a work shape");
   const bool far = g->mode == SR_MODE_FAR;
   const int K = c->points_per_lane, L = c->lanes_per_direction, st = c->steps_per_stage;
-  if (far ? (K != 8 && K != 16 && K != 24 && K != 32) : (K != 8))
-    return fail(SR_ERR_INVALID, "points per lane %d (far: 8, 16, 24, 32; near: 8)", K);
+  if (far ? (K != 8 && K != 16 && K != 24 && K != 32) : (K != 8 && K != 16))
+    return fail(SR_ERR_INVALID, "points per lane %d (far: 8, 16, 24, 32; near: 8, 16)", K);
   if (L != 8 && L != 16 && L != 32)
     return fail(SR_ERR_INVALID, "lanes per direction %d (8, 16 or 32)", L);
   if (far && (st < 32 || st > 512 || (st & 31) != 0))
@@ -159,7 +159,7 @@ extern "C" int sr_config_set(const sr_tracks *t, const sr_grid *g, int comp, int
   const FarMixedConfig cfg =
       far ? far_mixed_make(g->n_omega, n_dirs, t->n_tracks, device_sm_count(), K, L, st,
                            c->track_subsets)
-          : near_mixed_make(g->n_omega, n_dirs, t->n_tracks, device_sm_count(), L,
+          : near_mixed_make(g->n_omega, n_dirs, t->n_tracks, device_sm_count(), K, L,
                             c->track_subsets);
   std::lock_guard<std::mutex> lk(g_tmu);
   g_cache[key_of(t, g, comp)] = cfg;
@@ -222,16 +222,17 @@ extern "C" int sr_autotune(const sr_tracks *t, const sr_grid *g, int comp, int p
         kl.push_back(far_mixed_make(g->n_omega, n_dirs, n_s, n_sm, K, L, dflt.stage, 0));
       }
   } else {
-    for (int L : {32, 16, 8}) {
-      const uint64_t tile = (uint64_t)dflt.K * L;
-      const uint64_t tiles = (g->n_omega + tile - 1) / tile;
-      if ((double)(tiles * tile) > 1.34 * g->n_omega + 8.0 * L) continue;
-      kl.push_back(near_mixed_make(g->n_omega, n_dirs, n_s, n_sm, L, 0));
-    }
+    for (int K : {16, 8})
+      for (int L : {32, 16, 8}) {
+        const uint64_t tile = (uint64_t)K * L;
+        const uint64_t tiles = (g->n_omega + tile - 1) / tile;
+        if ((double)(tiles * tile) > 1.34 * g->n_omega + 8.0 * L) continue;
+        kl.push_back(near_mixed_make(g->n_omega, n_dirs, n_s, n_sm, K, L, 0));
+      }
   }
   const FarMixedConfig dflt_s =
       far ? far_mixed_make(g->n_omega, n_dirs, n_s, n_sm, dflt.K, dflt.L, dflt.stage, 0)
-          : near_mixed_make(g->n_omega, n_dirs, n_s, n_sm, dflt.L, 0);
+          : near_mixed_make(g->n_omega, n_dirs, n_s, n_sm, dflt.K, dflt.L, 0);
   kl.insert(kl.begin(), dflt_s);  // the default is always timed, first
 
   // scratch: outputs and the largest workspace any candidate can need
@@ -296,7 +297,7 @@ extern "C" int sr_autotune(const sr_tracks *t, const sr_grid *g, int comp, int p
       if (v < 1 || v > 64 || v > (int)n_s || v == h || elapsed_ms() > budget_ms) continue;
       FarMixedConfig c =
           far ? far_mixed_make(g->n_omega, n_dirs, n_s, n_sm, best.K, best.L, best.stage, v)
-              : near_mixed_make(g->n_omega, n_dirs, n_s, n_sm, best.L, v);
+              : near_mixed_make(g->n_omega, n_dirs, n_s, n_sm, best.K, best.L, v);
       const int before = best.n_sub;
       rc = consider(c);
       if (rc) break;
@@ -321,11 +322,12 @@ extern "C" int sr_autotune(const sr_tracks *t, const sr_grid *g, int comp, int p
   } else {
     const FarMixedConfig h = far ? far_mixed_make(g->n_omega, n_dirs, t->n_tracks, n_sm, best.K,
                                                   best.L, best.stage, 0)
-                                 : near_mixed_make(g->n_omega, n_dirs, t->n_tracks, n_sm, best.L, 0);
+                                 : near_mixed_make(g->n_omega, n_dirs, t->n_tracks, n_sm, best.K,
+                                                   best.L, 0);
     const int nsub = std::max(1, std::min(64, h.n_sub * sub_scale_num / sub_scale_den));
     chosen = far ? far_mixed_make(g->n_omega, n_dirs, t->n_tracks, n_sm, best.K, best.L,
                                   best.stage, nsub)
-                 : near_mixed_make(g->n_omega, n_dirs, t->n_tracks, n_sm, best.L, nsub);
+                 : near_mixed_make(g->n_omega, n_dirs, t->n_tracks, n_sm, best.K, best.L, nsub);
   }
   {
     std::lock_guard<std::mutex> lk(g_tmu);

@@ -93,6 +93,37 @@ def test_golden_mixed_near(name):
     compare(calc.Data["radiation"], case.expected, TOL["mixed"], name)
 
 
+@pytest.mark.parametrize("K", [8, 16])
+@pytest.mark.parametrize("name", [n for n in gc.names()
+                                  if n.startswith("near_") and not n.endswith("_float")])
+def test_golden_mixed_near_points_per_lane(name, K):
+    """Both near-field work shapes (8 and 16 omega points per lane) on every
+    near-field case: the shape is pinned for the case's sizes before the call."""
+    _need_gpu()
+    from synchrad_gb300 import _lib
+    from synchrad_gb300 import batch as bt
+    from synchrad_gb300.calc import VEC_COMPS
+    case = gc.load(name)
+    calc = run_case(case, dtype="mixed")  # the grid and the batch sizes of the call
+    it_range = case.call.get("it_range")
+    n_snaps = int(case.call.get("nSnaps", 1))
+    batch = bt.pack_tracks(case.fresh_tracks(), np.float64, n_snaps, case.call["timeStep"],
+                           it_range=it_range, device="cuda")
+    comp = case.call.get("comp", "total")
+    L = 32
+    while L > 8 and (L // 2) * K >= int(calc.Args["gridNodeNums"][0]):
+        L //= 2
+    try:
+        bt.set_config(batch, calc._grid_dev, comp, _lib.SR_PREC_MIXED, points_per_lane=K,
+                      lanes_per_direction=L)
+        assert bt.current_config(batch, calc._grid_dev, comp)["points_per_lane"] == K
+        calc2 = run_case(case, dtype="mixed")
+        assert sorted(calc2.Data["radiation"]) == sorted(VEC_COMPS[comp])
+        compare(calc2.Data["radiation"], case.expected, TOL["mixed"], f"{name} K={K}")
+    finally:
+        _lib.lib().sr_config_clear()
+
+
 def test_mixed_is_deterministic():
     _need_gpu()
     case = gc.load("far_total_ragged_wmean")

@@ -54,7 +54,7 @@ def test_fixed_chunking_is_reproducible_and_matches_one_call():
     def streamed():
         out = torch.zeros(shape, dtype=torch.float64, device="cuda")
         ts = bt.TrackStream("cuda")
-        for batch, _ in ts.chunks(w.tracks, np.float64, 1, w.time_step, plan=plan):
+        for batch, _, _ in ts.chunks(w.tracks, np.float64, 1, w.time_step, plan=plan):
             bt.run_spectrum(batch, grid, "total", prec, [out], check_status=True)
         torch.cuda.synchronize()
         return out.cpu().numpy()
