@@ -57,6 +57,9 @@ def parse():
                          "tracks on a screen at 20 undulator lengths; ragged: 8192 FP32 "
                          "betatron tracks of 500-20000 steps; adjoint: forward and "
                          "backward of sum(g * S) for 256 tracks x 2000 steps on 128 x 32 x 32")
+    ap.add_argument("--forward-precision", default="mixed", choices=["mixed", "double-float"],
+                    help="adjoint workloads: arithmetic of the differentiable forward "
+                         "(double-float: FP64-class spectrum, far field)")
     ap.add_argument("--tracks", type=int, default=None)
     ap.add_argument("--seed", type=int, default=0,
                     help="seed of the synthetic tracks (numpy default_rng)")
@@ -382,7 +385,8 @@ def adjoint_main(args):
     mode = w.args.get("mode", "far")
     lengths = [len(t[0]) for t in w.tracks]
     layout = make_layout(lengths, w.time_step, calc._host_axes, (nO, nT, nP), device,
-                         mode=mode, L_screen=w.L_screen or 0.0)
+                         mode=mode, L_screen=w.L_screen or 0.0,
+                         precision=args.forward_precision)
     spectrum = total_spectrum_fn(mode)
     coords = [torch.tensor(np.concatenate([np.asarray(t[c], np.float64) for t in w.tracks]),
                            device=device, requires_grad=True) for c in range(6)]
@@ -413,7 +417,7 @@ def adjoint_main(args):
     stream = torch.cuda.current_stream(device)
     pt_steps = w.pt_steps
     tune = None
-    if not args.no_tune:  # the forward's work shape, as for the forward benchmark
+    if not args.no_tune and args.forward_precision == "mixed":  # the forward's work shape
         from synchrad_gb300.autograd import _tracks_struct
         from synchrad_gb300.batch import autotune
         t0 = time.perf_counter()
@@ -488,12 +492,16 @@ def adjoint_main(args):
                 "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None,
-                "dtype": "f32 (mixed: double-float phase, FP32 sums, FP64 gradients)",
+                "dtype": ("f32 (mixed: double-float phase, FP32 sums, FP64 gradients)"
+                          if args.forward_precision == "mixed" else
+                          "double-float forward (~48-bit, FP32 pipe); mixed adjoint, FP64 "
+                          "gradients"),
                 "data": "synthetic",
                 "config": {"workload": w.name, "n_tracks": len(w.tracks), "seed": args.seed,
                            "steps_per_track": int(lengths[0]), "grid": [nO, nT, nP],
                            "pt_steps_per_step": pt_steps,
                            "loss": loss_name,
+                           "forward_precision": args.forward_precision,
                            "l2": "flushed before every timed step (256 MB write, counted)",
                            "parallelism": f"replicas x{ws} (tracks independent)"},
                 "adjoint": {"forward_ms": fwd_ms, "backward_ms": bwd_ms,

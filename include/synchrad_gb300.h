@@ -54,7 +54,10 @@ enum {
   SR_PREC_DOUBLE = 0,       /* FP64 throughout: the plain port of the reference kernel */
   SR_PREC_FLOAT = 1,        /* FP32 throughout: the reference's dtype='float' */
   SR_PREC_FLOAT_NATIVE = 2, /* FP32 with fast intrinsics: dtype='float' + 'native' */
-  SR_PREC_MIXED = 3         /* FP32 bulk, double-float phase, compensated sums, FP64 spectrum */
+  SR_PREC_MIXED = 3,        /* FP32 bulk, double-float phase, compensated sums, FP64 spectrum */
+  SR_PREC_DF = 4            /* double-float throughout (~48 bits) on the FP32 pipe: FP64-class
+                               spectra for losses that amplify the forward error; far field,
+                               F64 grid, F64 or F32 tracks.  No counterpart in the reference. */
 };
 
 /*
@@ -230,6 +233,14 @@ void sr_graph_destroy(sr_graph *graph);
 int sr_far_total_forward_saved(const sr_tracks *tracks, const sr_grid *grid,
                                double *spectrum, float *saved_A, void *workspace,
                                size_t workspace_bytes, void *stream);
+
+/* The same in double-float arithmetic (SR_PREC_DF): the spectrum to FP64-class
+ * accuracy, saved_A (float) as above.  Workspace: sr_workspace_bytes(...,
+ * SR_COMP_TOTAL, SR_PREC_DF).  For losses that amplify the forward error, such
+ * as a misfit S - T that is a small fraction of S. */
+int sr_far_total_forward_saved_df(const sr_tracks *tracks, const sr_grid *grid,
+                                  double *spectrum, float *saved_A, void *workspace,
+                                  size_t workspace_bytes, void *stream);
 
 /* Scratch bytes of sr_far_total_backward for these sizes. */
 int64_t sr_far_total_backward_workspace_bytes(const sr_tracks *tracks,

@@ -24,6 +24,7 @@ SOURCES = {
     "sr_api.cu": [],
     "sr_port.cu": ["--fmad=false"],
     "sr_far_mixed.cu": [],
+    "sr_far_df.cu": [],
     "sr_near_mixed.cu": [],
     "sr_far_adjoint.cu": [],
     "sr_diag.cu": [],

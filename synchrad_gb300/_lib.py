@@ -37,6 +37,7 @@ SR_PREC_DOUBLE = 0
 SR_PREC_FLOAT = 1
 SR_PREC_FLOAT_NATIVE = 2
 SR_PREC_MIXED = 3
+SR_PREC_DF = 4
 
 
 class SynchRadError(RuntimeError):
@@ -107,7 +108,7 @@ EXPORTS = (
     "sr_far_spheric_comps_complex", "sr_near_total", "sr_near_cartesian_comps",
     "sr_near_cartesian_comps_complex", "sr_timing_enable", "sr_timing_read",
     "sr_probe_fp32_peak", "sr_spectrum_noalloc", "sr_noalloc_status",
-    "sr_far_total_forward_saved",
+    "sr_far_total_forward_saved", "sr_far_total_forward_saved_df",
     "sr_far_total_backward_workspace_bytes", "sr_far_total_backward",
     "sr_autotune", "sr_config_get", "sr_config_set", "sr_config_clear", "sr_graph_create", "sr_graph_launch",
     "sr_graph_nodes", "sr_graph_destroy", "sr_near_total_forward_saved",
@@ -132,6 +133,9 @@ def _declare(L: ctypes.CDLL) -> None:
     L.sr_far_total_forward_saved.restype = i32
     L.sr_far_total_forward_saved.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid),
                                              vp, vp, vp, ctypes.c_size_t, vp]
+    L.sr_far_total_forward_saved_df.restype = i32
+    L.sr_far_total_forward_saved_df.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid),
+                                                vp, vp, vp, ctypes.c_size_t, vp]
     L.sr_far_total_backward_workspace_bytes.restype = ctypes.c_int64
     L.sr_far_total_backward_workspace_bytes.argtypes = [ctypes.POINTER(SrTracks),
                                                         ctypes.POINTER(SrGrid)]

@@ -2,7 +2,8 @@
 adjoint kernels.
 
 ``far_total_spectrum(x, y, z, ux, uy, uz, w, layout)`` and
-``near_total_spectrum(...)`` return the mixed-precision far-field or near-field
+``near_total_spectrum(...)`` return the mixed-precision (or, far field,
+double-float: ``make_layout(precision=...)``) far-field or near-field
 (screen) spectrum ``S`` (comp 'total', one snapshot, device layout
 ``[nPhi, nTheta|nR, nOmega]``) of a batch of tracks given as concatenated
 float64 CUDA tensors (CSR order of ``layout.offsets``); the backward calls
@@ -36,6 +37,7 @@ class SpectrumLayout:
     grid: GridDevice
     workspace: Workspace
     mode: str = "far"
+    precision: str = "mixed"     # forward arithmetic: 'mixed' or 'double-float' (far field)
 
     @property
     def n_tracks(self) -> int:
@@ -50,11 +52,20 @@ FarLayout = SpectrumLayout
 
 
 def make_layout(lengths, dt, host_axes, n, device="cuda", mode="far",
-                L_screen=0.0) -> SpectrumLayout:
+                L_screen=0.0, precision="mixed") -> SpectrumLayout:
     """Layout for tracks of the given lengths with the reference's per-track
     rules (it_start = 0, itEnd = length, one snapshot at the last step).
     host_axes: far (omega2pi, sinT, cosT, sinP, cosP), near (omega2pi, R,
-    sinP, cosP) as from ``synchrad/calc.py:486-512``."""
+    sinP, cosP) as from ``synchrad/calc.py:486-512``.
+
+    ``precision`` is the forward's arithmetic: 'mixed' (FP32 bulk, ~1e-7 of
+    the spectrum) or 'double-float' (far field, FP64-class spectrum), for
+    losses that amplify the spectrum's error, such as a misfit S - T that is a
+    small fraction of S.  The backward is the same for both."""
+    if precision not in ("mixed", "double-float"):
+        raise ValueError(f"precision {precision!r}: 'mixed' or 'double-float'")
+    if precision == "double-float" and mode != "far":
+        raise ValueError("the double-float forward is far field only")
     device = torch.device(device)
     lengths = np.asarray(lengths, dtype=np.int64)
     if np.any(lengths < 1):
@@ -67,7 +78,7 @@ def make_layout(lengths, dt, host_axes, n, device="cuda", mode="far",
     return SpectrumLayout(t(offsets), t(np.zeros(lengths.size, np.int32)),
                           t(lengths.astype(np.uint32).view(np.int32)),
                           t(snaps.astype(np.uint32).view(np.int32)), float(dt), grid,
-                          Workspace(device), mode)
+                          Workspace(device), mode, precision)
 
 
 def _tracks_struct(coords, w, layout: FarLayout) -> TrackBatch:
@@ -95,12 +106,14 @@ class TotalSpectrum(torch.autograd.Function):
         spec = torch.zeros((nP, nT, nO), dtype=torch.float64, device=x.device)
         saved = torch.empty(layout.n_tracks * P * _SAVED_FLOATS[layout.mode], dtype=torch.float32,
                             device=x.device)
-        need = L.sr_workspace_bytes(ctypes.byref(ts), ctypes.byref(gs), 0, _lib.SR_PREC_MIXED)
+        df_fwd = layout.precision == "double-float"
+        prec = _lib.SR_PREC_DF if df_fwd else _lib.SR_PREC_MIXED
+        need = L.sr_workspace_bytes(ctypes.byref(ts), ctypes.byref(gs), 0, prec)
         if need < 0:
             _lib.check(_lib.SR_ERR_INVALID if need == -1 else int(need))
         ws = layout.workspace.get(max(int(need), 256))
         stream = ctypes.c_void_p(torch.cuda.current_stream(x.device).cuda_stream)
-        fwd = getattr(L, f"sr_{layout.mode}_total_forward_saved")
+        fwd = getattr(L, f"sr_{layout.mode}_total_forward_saved" + ("_df" if df_fwd else ""))
         _lib.check(fwd(ctypes.byref(ts), ctypes.byref(gs), spec.data_ptr(), saved.data_ptr(),
                        ws.data_ptr(), ctypes.c_size_t(int(need)), stream))
         ctx.save_for_backward(*coords, wd, saved)

@@ -309,7 +309,10 @@ def precision_id(dtype_name: str, native: bool) -> int:
         return _lib.SR_PREC_FLOAT_NATIVE if native else _lib.SR_PREC_FLOAT
     if dtype_name == "mixed":
         return _lib.SR_PREC_MIXED
-    raise ValueError(f"unknown dtype {dtype_name!r} (expected 'double', 'float' or 'mixed')")
+    if dtype_name == "double-float":
+        return _lib.SR_PREC_DF
+    raise ValueError(f"unknown dtype {dtype_name!r} "
+                     "(expected 'double', 'float', 'mixed' or 'double-float')")
 
 
 class Workspace:

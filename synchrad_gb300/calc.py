@@ -6,7 +6,9 @@ arrays (``self.Data['radiation'][key]``, float64, shape
 and HDF5 layout as ``synchrad/calc.py``.  ``Args['dtype']`` keeps the
 reference's meanings ('double': the plain FP64 kernel, 'float': FP32, with
 ``Args['native']`` for the fast intrinsics) and adds 'mixed': FP32 bulk
-arithmetic with double-float phase and compensated sums, FP64 results.
+arithmetic with double-float phase and compensated sums, FP64 results; and
+'double-float': double-float arithmetic throughout (far field), FP64-class
+results on the FP32 pipe.
 
 Differences from the reference, all deliberate:
   * one batched GPU call per ``calculate_spectrum`` instead of one OpenCL
@@ -143,7 +145,7 @@ class SynchRad(Utilities):
             np_dtype = np.float32
         elif name == "double":
             np_dtype = np.float64
-        else:  # mixed: FP32 tracks stay FP32 (C3-style inputs), others FP64
+        else:  # mixed, double-float: FP32 tracks stay FP32, others FP64
             all32 = all(np.asarray(t[k]).dtype == np.float32 for t in tracks for k in range(6))
             np_dtype = np.float32 if all32 else np.float64
         if it_range is None:
@@ -263,7 +265,7 @@ class SynchRad(Utilities):
             self.Args["mode"] = "far"
         if "dtype" not in self.Args:
             self.Args["dtype"] = "double"
-        if self.Args["dtype"] in ("double", "mixed"):
+        if self.Args["dtype"] in ("double", "mixed", "double-float"):
             self.dtype = np.double
         elif self.Args["dtype"] == "float":
             self.dtype = np.single
@@ -271,6 +273,8 @@ class SynchRad(Utilities):
             raise ValueError(f"unknown dtype {self.Args['dtype']!r}")
         if self.Args["mode"] not in ("far", "near"):
             raise ValueError(f"unknown mode {self.Args['mode']!r}")
+        if self.Args["dtype"] == "double-float" and self.Args["mode"] != "far":
+            raise ValueError("dtype 'double-float' evaluates the far field only")
         if self.Args["dtype"] == "float":
             if self.Args["mode"] == "far":
                 print("WARNING: Chosen single precision should be "

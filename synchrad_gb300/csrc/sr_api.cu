@@ -46,7 +46,7 @@ int check_common(const sr_tracks *t, const sr_grid *g, int comp, int precision,
   if (nout == 0) return fail(SR_ERR_INVALID, "unknown comp %d", comp);
   if (g->mode == SR_MODE_NEAR && comp > SR_COMP_CARTESIAN_COMPLEX)
     return fail(SR_ERR_INVALID, "comp %d is far-field only (spheric components)", comp);
-  if (precision < SR_PREC_DOUBLE || precision > SR_PREC_MIXED)
+  if (precision < SR_PREC_DOUBLE || precision > SR_PREC_DF)
     return fail(SR_ERR_INVALID, "unknown precision %d", precision);
   if (t->dtype > SR_DTYPE_F32 || g->dtype > SR_DTYPE_F32)
     return fail(SR_ERR_INVALID, "unknown dtype");
@@ -57,6 +57,10 @@ int check_common(const sr_tracks *t, const sr_grid *g, int comp, int precision,
     return fail(SR_ERR_INVALID, "SR_PREC_FLOAT needs FP32 tracks and grid");
   if (precision == SR_PREC_MIXED && g->dtype != SR_DTYPE_F64)
     return fail(SR_ERR_INVALID, "SR_PREC_MIXED needs an FP64 grid");
+  if (precision == SR_PREC_DF && g->dtype != SR_DTYPE_F64)
+    return fail(SR_ERR_INVALID, "SR_PREC_DF needs an FP64 grid");
+  if (precision == SR_PREC_DF && g->mode != SR_MODE_FAR)
+    return fail(SR_ERR_UNSUPPORTED, "SR_PREC_DF evaluates the far field only");
   if (!out) return fail(SR_ERR_INVALID, "out must not be NULL");
   for (int i = 0; i < nout; ++i)
     if (!out[i]) return fail(SR_ERR_INVALID, "output array %d is NULL", i);
@@ -140,10 +144,17 @@ extern "C" int64_t sr_workspace_bytes(const sr_tracks *t, const sr_grid *g, int 
   if (nout == 0) return fail(SR_ERR_INVALID, "unknown comp %d", comp);
   if (g->mode == SR_MODE_NEAR && comp > SR_COMP_CARTESIAN_COMPLEX)
     return fail(SR_ERR_INVALID, "comp %d is far-field only (spheric components)", comp);
-  if (precision < SR_PREC_DOUBLE || precision > SR_PREC_MIXED)
+  if (precision < SR_PREC_DOUBLE || precision > SR_PREC_DF)
     return fail(SR_ERR_INVALID, "unknown precision %d", precision);
-  if (precision != SR_PREC_MIXED) return 0;
   const uint64_t P = (uint64_t)g->n_omega * g->n_theta * g->n_phi;
+  if (precision == SR_PREC_DF) {
+    if (g->mode != SR_MODE_FAR)
+      return fail(SR_ERR_UNSUPPORTED, "SR_PREC_DF evaluates the far field only");
+    const FarMixedConfig cfg =
+        far_df_choose(g->n_omega, g->n_theta * g->n_phi, t->n_tracks, device_sm_count());
+    return (int64_t)far_df_workspace(t->total_steps, P, nout, t->n_snaps ? t->n_snaps : 1, cfg);
+  }
+  if (precision != SR_PREC_MIXED) return 0;
   const FarMixedConfig cfg = mixed_config(t, g, comp);
   if (g->mode == SR_MODE_FAR)
     return (int64_t)far_mixed_workspace(t->total_steps, P, nout, t->n_snaps ? t->n_snaps : 1, cfg);
@@ -173,6 +184,11 @@ extern "C" int sr_spectrum(const sr_tracks *t, const sr_grid *g, int comp, int p
   if (P == 0 || t->n_tracks == 0 || t->n_snaps == 0) return SR_OK;
   cudaStream_t s = (cudaStream_t)stream;
 
+  if (precision == SR_PREC_DF) {
+    const FarMixedConfig cfg =
+        far_df_choose(g->n_omega, g->n_theta * g->n_phi, t->n_tracks, device_sm_count());
+    return launch_far_df(far_mixed_params(t, g, comp, out), cfg, workspace, workspace_bytes, s);
+  }
   if (precision == SR_PREC_MIXED) {
     const FarMixedConfig cfg = mixed_config(t, g, comp);
     if (g->mode == SR_MODE_FAR)

@@ -467,6 +467,26 @@ extern "C" int sr_far_total_forward_saved(const sr_tracks *t, const sr_grid *g, 
   return launch_far_mixed(p, cfg, workspace, workspace_bytes, s);
 }
 
+extern "C" int sr_far_total_forward_saved_df(const sr_tracks *t, const sr_grid *g,
+                                             double *spectrum, float *saved_A, void *workspace,
+                                             size_t workspace_bytes, void *stream) {
+  clear_error();
+  void *out[6] = {spectrum};
+  int rc = check_adjoint_args(t, g, out);
+  if (rc) return rc;
+  if (!saved_A) return fail(SR_ERR_INVALID, "saved_A is NULL");
+  const uint64_t P = (uint64_t)g->n_omega * g->n_theta * g->n_phi;
+  if (P == 0 || t->n_tracks == 0) return SR_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaMemsetAsync(saved_A, 0, (size_t)t->n_tracks * P * 16, s);
+  if (e != cudaSuccess) return cuda_fail(e, "saved_A reset");
+  const FarMixedConfig cfg =
+      far_df_choose(g->n_omega, g->n_theta * g->n_phi, t->n_tracks, device_sm_count());
+  FarMixedParams p = make_far_mixed_params(t, g, SR_COMP_TOTAL, out);
+  p.save_A = saved_A;
+  return launch_far_df(p, cfg, workspace, workspace_bytes, s);
+}
+
 extern "C" int64_t sr_far_total_backward_workspace_bytes(const sr_tracks *t, const sr_grid *g) {
   if (!t || !g) return -1;
   const uint64_t n_dirs = (uint64_t)g->n_theta * g->n_phi;

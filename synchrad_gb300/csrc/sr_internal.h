@@ -109,6 +109,14 @@ size_t near_mixed_workspace(int64_t total_steps, uint64_t n_points, int n_out,
 int launch_near_mixed(FarMixedParams p, const FarMixedConfig &cfg, void *workspace,
                       size_t ws_bytes, cudaStream_t stream);
 
+// The double-float far field (sr_far_df.cu, SR_PREC_DF): its work shape,
+// workspace size and launch (same parameter block as the mixed far field).
+FarMixedConfig far_df_choose(uint32_t n_omega, uint32_t n_dirs, uint32_t n_tracks, int n_sm);
+size_t far_df_workspace(int64_t total_steps, uint64_t n_points, int n_out, uint32_t n_snaps,
+                        const FarMixedConfig &cfg);
+int launch_far_df(FarMixedParams p, const FarMixedConfig &cfg, void *workspace,
+                  size_t ws_bytes, cudaStream_t stream);
+
 // sr_api.cu: argument checks and parameter packing shared by entry points.
 int validate_spectrum_args(const sr_tracks *t, const sr_grid *g, int comp,
                            int precision, void *const *out);

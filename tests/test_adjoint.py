@@ -318,7 +318,9 @@ def test_misfit_loss_matches_finite_differences():
       and passed to the backward: TOL_ADJ_FD;
     * end to end (mixed forward, autograd of the loss, adjoint): S - T is about
       1e-3 of S, so the ~1e-6 relative error of the mixed spectrum enters
-      dL/dS amplified a thousandfold: TOL_MISFIT_E2E.
+      dL/dS amplified a thousandfold: TOL_MISFIT_E2E;
+    * end to end with the double-float forward (``make_layout(precision=
+      'double-float')``), whose spectrum is FP64-class: TOL_ADJ_FD.
     """
     _need_gpu()
     from synchrad_gb300.autograd import far_total_spectrum, make_layout
@@ -331,19 +333,21 @@ def test_misfit_loss_matches_finite_differences():
     per_track = [oracle_track_spectrum(t[:6], t[6], dt, axes, n) for t in tracks]
     total = sum(per_track)
 
-    def gradients(grad_from_fp64):
+    layout_df = make_layout(lengths, dt, axes, n, precision="double-float")
+
+    def gradients(grad_from_fp64, lay=layout):
         ts = [torch.tensor(c, dtype=torch.float64, device="cuda", requires_grad=True)
               for c in coords]
         w = torch.tensor(weights, dtype=torch.float64, device="cuda", requires_grad=True)
-        S = far_total_spectrum(*ts, w, layout)
+        S = far_total_spectrum(*ts, w, lay)
         if grad_from_fp64:
             S.backward(torch.tensor(2.0 * (total - target) * inv * inv, device="cuda"))
         else:
             (((S - torch.tensor(target, device="cuda")) * inv) ** 2).sum().backward()
         return [t.grad.cpu().numpy() for t in ts]
 
-    g64, gmx = gradients(True), gradients(False)
-    got64, gotmx, exp = [], [], []
+    g64, gmx, gdf = gradients(True), gradients(False), gradients(False, layout_df)
+    got64, gotmx, gotdf, exp = [], [], [], []
     for (t, c, s) in pick_coordinates(tracks, 32, seed=23):
         base = tracks[t]
         v = base[c][s]
@@ -359,7 +363,10 @@ def test_misfit_loss_matches_finite_differences():
         exp.append((8.0 * (L_of(h) - L_of(-h)) - (L_of(2 * h) - L_of(-2 * h))) / (12.0 * h))
         got64.append(g64[c][offsets[t] + s])
         gotmx.append(gmx[c][offsets[t] + s])
-    e64, emx = rel_l2(got64, exp), rel_l2(gotmx, exp)
-    print(f"misfit loss vs finite differences: adjoint {e64:.2e}, end to end {emx:.2e}")
+        gotdf.append(gdf[c][offsets[t] + s])
+    e64, emx, edf = rel_l2(got64, exp), rel_l2(gotmx, exp), rel_l2(gotdf, exp)
+    print(f"misfit loss vs finite differences: adjoint {e64:.2e}, end to end {emx:.2e} "
+          f"(mixed forward), {edf:.2e} (double-float forward)")
     assert e64 <= TOL_ADJ_FD
     assert emx <= TOL_MISFIT_E2E
+    assert edf <= TOL_ADJ_FD

@@ -8,6 +8,9 @@ arrays carrying more than 1e-6 of the comp's norm):
     FP32 sin/cos of the GPU and of glibc differ by an ulp or two.
   * dtype 'mixed' against the FP64 golden vectors: 1e-5 (the target accuracy
     of the mixed-precision path).
+  * dtype 'double-float' (far field) against the FP64 golden vectors: 1e-10
+    (about 48-bit arithmetic; the reference's own FP64 phase carries ~1e-9 rad
+    at the largest phases, which averages down in the sums).
 """
 import ctypes
 
@@ -19,7 +22,7 @@ import golden_cases as gc
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
-TOL = {"double": 1e-12, "float": 1e-5, "mixed": 1e-5}
+TOL = {"double": 1e-12, "float": 1e-5, "mixed": 1e-5, "double-float": 1e-10}
 
 
 def _need_gpu():
@@ -91,6 +94,17 @@ def test_golden_mixed_near(name):
     case = gc.load(name)
     calc = run_case(case, dtype="mixed")
     compare(calc.Data["radiation"], case.expected, TOL["mixed"], name)
+
+
+@pytest.mark.parametrize("name", [n for n in gc.names()
+                                  if n.startswith("far_") and not n.endswith("_float")])
+def test_golden_double_float_far(name):
+    """Double-float arithmetic against the FP64 reference on every far-field case."""
+    _need_gpu()
+    case = gc.load(name)
+    calc = run_case(case, dtype="double-float")
+    rel = compare(calc.Data["radiation"], case.expected, TOL["double-float"], name)
+    print(f"{name}: double-float relative L2 {rel:.2e}")
 
 
 @pytest.mark.parametrize("K", [8, 16])
