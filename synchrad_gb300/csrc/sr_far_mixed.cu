@@ -162,6 +162,17 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
   const double inv2pi = 0.15915494309189533577;
   float *outer = p.outer + ((size_t)blockIdx.x * W + warp) * K * 8 * 32;
   uint32_t stage_no = 0;  // running stage counter (mbarrier phase bookkeeping)
+  // A uniform omega axis (omega_j = omega_0 + j d_omega to 1e-12): the points of
+  // a (direction, step) that pass the mask form one index interval, found once
+  // per (direction, step) in the setup and shared by the lanes.
+  bool axis_ok = nO < 65535u;
+  for (uint32_t j = threadIdx.x; j < nO && axis_ok; j += blockDim.x) {
+    const double wj = p.omega[j];
+    if (fabs(wj - (p.omega[0] + (double)j * dw_glob)) > 1e-12 * fabs(wj) + 1e-300) axis_ok = false;
+  }
+  const bool iv = __syncthreads_and(axis_ok) != 0;
+  const float w0g = nO > 0 ? (float)p.omega[0] : 0.f;
+  const float dwg = (float)dw_glob, inv_dwg = (dwg != 0.f) ? 1.0f / dwg : 0.f;
 
   for (uint32_t item = blockIdx.x; item < p.n_items; item += gridDim.x) {
     const uint32_t sub = item / p.n_groups, grp = item % p.n_groups;
@@ -421,7 +432,16 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
                 st[2 * 32] = make_float4(R2c, R2c, R2s, R2s);
                 st[3 * 32] = make_float4(-R2s, -R2s, Hc, Hc);
                 st[4 * 32] = make_float4(Hs, Hs, -Hs, -Hs);
-                st[5 * 32] = make_float4(fabsf(dtau), 0.f, 0.f, 0.f);
+                // the mask's index intervals over the whole omega axis: points
+                // certainly included (below kPiLo) and possibly included (kPiHi)
+                int jfc = 1, jlc = 0, jfu = 1, jlu = 0;
+                if (iv) {
+                  const float inv_adt = __frcp_rn(fabsf(dtau));
+                  omega_interval(w0g, dwg, inv_dwg, kPiLo * inv_adt, (int)nO, jfc, jlc);
+                  omega_interval(w0g, dwg, inv_dwg, kPiHi * inv_adt, (int)nO, jfu, jlu);
+                }
+                st[5 * 32] = make_float4(fabsf(dtau), __int_as_float(jfc), __int_as_float(jlc),
+                                         __uint_as_float((uint32_t)jfu | ((uint32_t)(jlu + 1) << 16)));
                 // largest |dtau| of the chunk: decides the chunk's fast loop
                 const float am = (uint32_t)lane < mcnt ? fabsf(dtau) : 0.f;
                 const float amax = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(am)));
@@ -487,10 +507,18 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
 #pragma unroll 1
               for (uint32_t i = 0; i < mcnt; ++i) {
                 const float4 *st = setup + (size_t)dsub * 6 * 32 + i;
-                const float adt = st[5 * 32].x;
+                const float4 M = st[5 * 32];
+                const float adt = M.x;
                 const uint32_t s = s0 + c0 + i;
-                const bool all_in = wabs_max * adt < kPiLo;
-                const bool all_out = wabs_min * adt > kPiHi;
+                const int jfc = __float_as_int(M.y), jlc = __float_as_int(M.z);
+                const uint32_t pu = __float_as_uint(M.w);
+                const int jfu = (int)(pu & 0xffffu), jlu = (int)(pu >> 16) - 1;
+                // a lane is all in (out) when the certain (possible) interval
+                // covers (misses) its points [j0, j0 + nv)
+                const bool all_in = iv ? (jfc <= j0 && jlc >= j0 + nv - 1)
+                                       : (wabs_max * adt < kPiLo);
+                const bool all_out = iv ? (jlu < j0 || jfu > j0 + nv - 1)
+                                        : (wabs_min * adt > kPiHi);
                 if (__all_sync(0xffffffffu, uniform && (all_in || nv == 0))) {
                   // every point of the warp included: the straight-line step
                   // (the same products as the masked path with a full mask)
@@ -505,13 +533,18 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
                   uint32_t mask = (all_out || nv == 0) ? 0u : 0xffffffffu;
                   if (!all_in && !all_out && nv > 0) {
                     const DirConst &d = sm.dc[warp][dsub];
-                    if (uniform) {
+                    if (iv || uniform) {
                       // included points form an index interval; only points
                       // inside the guard band need the exact FP64 test
-                      const float inv_adt = __frcp_rn(adt);  // adt > 0 here
-                      mask = omega_range_bits_r(w0f, dwf, inv_dwf, kPiLo * inv_adt, nv);
-                      uint32_t unc =
-                          omega_range_bits_r(w0f, dwf, inv_dwf, kPiHi * inv_adt, nv) & ~mask;
+                      uint32_t unc;
+                      if (iv) {
+                        mask = range_bits(jfc, jlc, j0, nv);
+                        unc = range_bits(jfu, jlu, j0, nv) & ~mask;
+                      } else {
+                        const float inv_adt = __frcp_rn(adt);  // adt > 0 here
+                        mask = omega_range_bits_r(w0f, dwf, inv_dwf, kPiLo * inv_adt, nv);
+                        unc = omega_range_bits_r(w0f, dwf, inv_dwf, kPiHi * inv_adt, nv) & ~mask;
+                      }
                       while (unc) {
                         const int m = __ffs(unc) - 1;
                         unc &= unc - 1u;

@@ -131,6 +131,42 @@ __device__ __forceinline__ uint32_t omega_range_bits_r(float w0, float dw, float
   return upto & ~below & all;
 }
 
+// Indices j in [0, n) of a uniform omega axis (omega_j = w0 + j dw) with
+// |omega_j| < wb: an interval [jf, jl] (empty when jf > jl), from its two float
+// bounds.  Float rounding of w0, dw and the products moves the bounds by about
+// 1e-7 of |omega| at the bound, inside the 4e-6 guard band between kPiLo and
+// kPiHi whose points are tested exactly.
+__device__ __forceinline__ void omega_interval(float w0, float dw, float inv_dw, float wb, int n,
+                                               int &jf, int &jl) {
+  jf = 1;
+  jl = 0;
+  if (!(wb > 0.f)) return;
+  float lo, hi;
+  if (dw > 0.f) {
+    lo = (-wb - w0) * inv_dw;
+    hi = (wb - w0) * inv_dw;
+  } else if (dw < 0.f) {
+    lo = (wb - w0) * inv_dw;
+    hi = (-wb - w0) * inv_dw;
+  } else {
+    if (fabsf(w0) < wb) { jf = 0; jl = n - 1; }
+    return;
+  }
+  const float top = (float)n + 1.f;
+  lo = fminf(fmaxf(lo, -2.f), top);
+  hi = fminf(fmaxf(hi, -2.f), top);
+  jf = max(0, (int)floorf(lo) + 1);      // first j > lo
+  jl = min(n - 1, (int)ceilf(hi) - 1);   // last j < hi
+}
+
+// Bits (j - j0) of the indices j in [a, b] clamped to [j0, j0 + nv), nv <= 32.
+__device__ __forceinline__ uint32_t range_bits(int a, int b, int j0, int nv) {
+  const int lo = max(a, j0) - j0, hi = min(b, j0 + nv - 1) - j0;
+  if (lo > hi) return 0u;
+  const uint32_t upto = (hi >= 31) ? 0xffffffffu : ((2u << hi) - 1u);
+  return upto & ~((1u << lo) - 1u);
+}
+
 // (zr + i zi) * (rc + i rs) for two points at once, factors given as pairs.
 __device__ __forceinline__ void rot2p(float2 zr, float2 zi, float2 rc, float2 rs, float2 nrs,
                                       float2 &or_, float2 &oi) {

@@ -507,15 +507,16 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
                           if (e == 0) { zr.x = cc; zi.x = ss; } else { zr.y = cc; zi.y = ss; }
                         }
                       }
-                      const float g0 = ((mask >> m0) & 1u) ? 1.f : 0.f;
-                      const float g1 = ((mask >> (m0 + 1)) & 1u) ? 1.f : 0.f;
-                      const float2 aa[3] = {make_float2(F1.x * g0, F1.y * g1),
-                                            make_float2(F1.z * g0, F1.w * g1),
-                                            make_float2(F2.x * g0, F2.y * g1)};
-                      const float2 bb[3] = {make_float2(F2.z * g0, F2.w * g1),
-                                            make_float2(F3.x * g0, F3.y * g1),
-                                            make_float2(F3.z * g0, F3.w * g1)};
-                      near_accumulate(acc, h * HP + q, zr, zi, bb, aa);
+                      // masked points: their phasors (not the six amplitudes)
+                      // are zeroed, one packed product per component
+                      const float2 g = make_float2(((mask >> m0) & 1u) ? 1.f : 0.f,
+                                                   ((mask >> (m0 + 1)) & 1u) ? 1.f : 0.f);
+                      const float2 aa[3] = {make_float2(F1.x, F1.y), make_float2(F1.z, F1.w),
+                                            make_float2(F2.x, F2.y)};
+                      const float2 bb[3] = {make_float2(F2.z, F2.w), make_float2(F3.x, F3.y),
+                                            make_float2(F3.z, F3.w)};
+                      near_accumulate(acc, h * HP + q, __fmul2_rn(zr, g), __fmul2_rn(zi, g), bb,
+                                      aa);
                     }
                     if (q + 1 < HP && uniform) {
                       rot2p(ZrA, ZiA, make_float2(R2.x, R2.y), make_float2(R2.z, R2.w),
