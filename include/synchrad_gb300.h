@@ -221,7 +221,7 @@ int sr_graph_nodes(const sr_graph *graph, int *n_kernels, int *n_nodes);
 void sr_graph_destroy(sr_graph *graph);
 
 /* ---------------------------------------------------------------------------
- * Adjoint of the mixed-precision far field, comp 'total', one snapshot.
+ * Adjoint of the far field (mixed or double-float forward), one snapshot.
  * No counterpart in the reference (it has no gradients).  The |dphase| < pi
  * mask is held fixed; uniform and non-uniform omega axes.
  * ------------------------------------------------------------------------- */
@@ -255,6 +255,25 @@ int sr_far_total_backward(const sr_tracks *tracks, const sr_grid *grid,
                           double *const *grad_track, double *grad_weight,
                           void *workspace, size_t workspace_bytes, void *stream);
 
+/* Every far-field comp (the reference's five far kernels,
+ * synchrad/kernel_farfield.cl:6-595), one snapshot: the forward of comp `comp`
+ * in `precision` (SR_PREC_MIXED or SR_PREC_DF) into its n_out outputs (double,
+ * accumulated), recording saved_A as above; workspace: sr_workspace_bytes of
+ * that comp and precision.  The backward takes dL/dS_k for each output
+ * (grad_out[k], [P] doubles) and writes the same gradients as
+ * sr_far_total_backward.  Quadratic comps (total, cartesian, spheric) and the
+ * coherent *_complex comps (linear in A: their dL/dw follows sqrt(w)); the
+ * spheric radial outputs are identically zero and carry no gradient.  Its
+ * workspace is sr_far_backward_workspace_bytes (the same for every comp). */
+int sr_far_forward_saved(const sr_tracks *tracks, const sr_grid *grid, int comp, int precision,
+                         void *const *out, float *saved_A, void *workspace,
+                         size_t workspace_bytes, void *stream);
+int64_t sr_far_backward_workspace_bytes(const sr_tracks *tracks, const sr_grid *grid);
+int sr_far_backward(const sr_tracks *tracks, const sr_grid *grid, int comp,
+                    const double *const *grad_out, const float *saved_A,
+                    double *const *grad_track, double *grad_weight, void *workspace,
+                    size_t workspace_bytes, void *stream);
+
 /* ---------------------------------------------------------------------------
  * Adjoint of the mixed-precision near field (screen at distance L), comp
  * 'total', one snapshot.  No counterpart in the reference.  Same conventions
@@ -270,6 +289,20 @@ int sr_near_total_backward(const sr_tracks *tracks, const sr_grid *grid,
                            const double *grad_spectrum, const float *saved_A,
                            double *const *grad_track, double *grad_weight,
                            void *workspace, size_t workspace_bytes, void *stream);
+
+/* Every near-field comp (total, cartesian, cartesian_complex:
+ * synchrad/kernel_nearfield.cl:5-326), one snapshot, as sr_far_forward_saved /
+ * sr_far_backward: outputs and their gradients per comp; saved_A as for
+ * sr_near_total_forward_saved.  cartesian_complex outputs (sqrt(w) dt Re/Im
+ * of e^{i omega L} A_k) are linear in A.  No counterpart in the reference. */
+int sr_near_forward_saved(const sr_tracks *tracks, const sr_grid *grid, int comp,
+                          void *const *out, float *saved_A, void *workspace,
+                          size_t workspace_bytes, void *stream);
+int64_t sr_near_backward_workspace_bytes(const sr_tracks *tracks, const sr_grid *grid);
+int sr_near_backward(const sr_tracks *tracks, const sr_grid *grid, int comp,
+                     const double *const *grad_out, const float *saved_A,
+                     double *const *grad_track, double *grad_weight, void *workspace,
+                     size_t workspace_bytes, void *stream);
 
 /* ---------------------------------------------------------------------------
  * Diagnostics.  These have no counterpart in the reference; the benchmark uses

@@ -108,12 +108,14 @@ EXPORTS = (
     "sr_far_spheric_comps_complex", "sr_near_total", "sr_near_cartesian_comps",
     "sr_near_cartesian_comps_complex", "sr_timing_enable", "sr_timing_read",
     "sr_probe_fp32_peak", "sr_spectrum_noalloc", "sr_noalloc_status",
-    "sr_far_total_forward_saved", "sr_far_total_forward_saved_df",
+    "sr_far_total_forward_saved", "sr_far_total_forward_saved_df", "sr_far_forward_saved",
+    "sr_far_backward_workspace_bytes", "sr_far_backward",
     "sr_far_total_backward_workspace_bytes", "sr_far_total_backward",
     "sr_autotune", "sr_config_get", "sr_config_set", "sr_config_clear", "sr_graph_create", "sr_graph_launch",
     "sr_graph_nodes", "sr_graph_destroy", "sr_near_total_forward_saved",
     "sr_near_total_backward_workspace_bytes", "sr_near_total_backward",
-    "sr_selftest_wait_timeout",
+    "sr_selftest_wait_timeout", "sr_near_forward_saved", "sr_near_backward_workspace_bytes",
+    "sr_near_backward",
 )
 
 _lock = threading.Lock()
@@ -133,6 +135,25 @@ def _declare(L: ctypes.CDLL) -> None:
     L.sr_far_total_forward_saved.restype = i32
     L.sr_far_total_forward_saved.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid),
                                              vp, vp, vp, ctypes.c_size_t, vp]
+    L.sr_far_forward_saved.restype = i32
+    L.sr_far_forward_saved.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid), i32, i32,
+                                       ctypes.POINTER(vp), vp, vp, ctypes.c_size_t, vp]
+    L.sr_far_backward_workspace_bytes.restype = ctypes.c_int64
+    L.sr_far_backward_workspace_bytes.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid)]
+    L.sr_far_backward.restype = i32
+    L.sr_far_backward.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid), i32,
+                                  ctypes.POINTER(vp), vp, ctypes.POINTER(vp), vp, vp,
+                                  ctypes.c_size_t, vp]
+    L.sr_near_forward_saved.restype = i32
+    L.sr_near_forward_saved.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid), i32,
+                                        ctypes.POINTER(vp), vp, vp, ctypes.c_size_t, vp]
+    L.sr_near_backward_workspace_bytes.restype = ctypes.c_int64
+    L.sr_near_backward_workspace_bytes.argtypes = [ctypes.POINTER(SrTracks),
+                                                   ctypes.POINTER(SrGrid)]
+    L.sr_near_backward.restype = i32
+    L.sr_near_backward.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid), i32,
+                                   ctypes.POINTER(vp), vp, ctypes.POINTER(vp), vp, vp,
+                                   ctypes.c_size_t, vp]
     L.sr_far_total_forward_saved_df.restype = i32
     L.sr_far_total_forward_saved_df.argtypes = [ctypes.POINTER(SrTracks), ctypes.POINTER(SrGrid),
                                                 vp, vp, vp, ctypes.c_size_t, vp]

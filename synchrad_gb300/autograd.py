@@ -52,7 +52,7 @@ FarLayout = SpectrumLayout
 
 
 def make_layout(lengths, dt, host_axes, n, device="cuda", mode="far",
-                L_screen=0.0, precision="mixed") -> SpectrumLayout:
+                L_screen=0.0, precision="mixed", form_factor=None) -> SpectrumLayout:
     """Layout for tracks of the given lengths with the reference's per-track
     rules (it_start = 0, itEnd = length, one snapshot at the last step).
     host_axes: far (omega2pi, sinT, cosT, sinP, cosP), near (omega2pi, R,
@@ -61,7 +61,9 @@ def make_layout(lengths, dt, host_axes, n, device="cuda", mode="far",
     ``precision`` is the forward's arithmetic: 'mixed' (FP32 bulk, ~1e-7 of
     the spectrum) or 'double-float' (far field, FP64-class spectrum), for
     losses that amplify the spectrum's error, such as a misfit S - T that is a
-    small fraction of S.  The backward is the same for both."""
+    small fraction of S.  The backward is the same for both.  ``form_factor``
+    (one value per omega, ``synchrad/calc.py:475-480``) is needed by the far
+    'cartesian_complex' comp."""
     if precision not in ("mixed", "double-float"):
         raise ValueError(f"precision {precision!r}: 'mixed' or 'double-float'")
     if precision == "double-float" and mode != "far":
@@ -74,7 +76,9 @@ def make_layout(lengths, dt, host_axes, n, device="cuda", mode="far",
     np.cumsum(lengths, out=offsets[1:])
     snaps = np.concatenate([snap_iterations((0, int(L)), 1) for L in lengths])
     t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)
-    grid = make_grid(mode, host_axes, n, torch.float64, device, L_screen=L_screen)
+    grid = make_grid(mode, host_axes, n, torch.float64, device, L_screen=L_screen,
+                     form_factor=None if form_factor is None
+                     else np.asarray(form_factor, dtype=np.float64))
     return SpectrumLayout(t(offsets), t(np.zeros(lengths.size, np.int32)),
                           t(lengths.astype(np.uint32).view(np.int32)),
                           t(snaps.astype(np.uint32).view(np.int32)), float(dt), grid,
@@ -144,6 +148,101 @@ class TotalSpectrum(torch.autograd.Function):
 
 
 FarTotalSpectrum = TotalSpectrum
+
+
+class SpectrumComps(torch.autograd.Function):
+    """Every comp of the far field or the near field (the layout's mode): the
+    forward returns the comp's outputs (the reference's keys in order, e.g.
+    x, y, z or xre, xim, ..., zim) and the backward takes a gradient for each
+    (None counts as zero)."""
+
+    @staticmethod
+    def forward(ctx, x, y, z, ux, uy, uz, w, layout: SpectrumLayout, comp: str):
+        L = _lib.lib()
+        cid = _lib.COMP_IDS[comp]
+        coords = [c.detach().contiguous() for c in (x, y, z, ux, uy, uz)]
+        for c in coords:
+            if c.dtype != torch.float64 or not c.is_cuda:
+                raise TypeError("track tensors must be float64 CUDA tensors")
+        wd = w.detach().contiguous().to(torch.float64)
+        batch = _tracks_struct(coords, wd, layout)
+        ts, gs = batch.c_struct(), layout.grid.c_struct()
+        nO, nT, nP = layout.grid.n
+        P = layout.n_points
+        outs = [torch.zeros((nP, nT, nO), dtype=torch.float64, device=x.device)
+                for _ in range(_lib.N_OUT[cid])]
+        saved = torch.empty(layout.n_tracks * P * _SAVED_FLOATS[layout.mode], dtype=torch.float32,
+                            device=x.device)
+        prec = _lib.SR_PREC_DF if layout.precision == "double-float" else _lib.SR_PREC_MIXED
+        need = L.sr_workspace_bytes(ctypes.byref(ts), ctypes.byref(gs), cid, prec)
+        if need < 0:
+            _lib.check(_lib.SR_ERR_INVALID if need == -1 else int(need))
+        ws = layout.workspace.get(max(int(need), 256))
+        ptrs = (ctypes.c_void_p * 6)(*([o.data_ptr() for o in outs] + [None] * (6 - len(outs))))
+        stream = ctypes.c_void_p(torch.cuda.current_stream(x.device).cuda_stream)
+        if layout.mode == "far":
+            rc = L.sr_far_forward_saved(ctypes.byref(ts), ctypes.byref(gs), cid, prec, ptrs,
+                                        saved.data_ptr(), ws.data_ptr(),
+                                        ctypes.c_size_t(int(need)), stream)
+        else:
+            rc = L.sr_near_forward_saved(ctypes.byref(ts), ctypes.byref(gs), cid, ptrs,
+                                         saved.data_ptr(), ws.data_ptr(),
+                                         ctypes.c_size_t(int(need)), stream)
+        _lib.check(rc)
+        ctx.save_for_backward(*coords, wd, saved)
+        ctx.layout = layout
+        ctx.comp = comp
+        return tuple(outs)
+
+    @staticmethod
+    def backward(ctx, *grad_outs):
+        L = _lib.lib()
+        *coords, wd, saved = ctx.saved_tensors
+        layout = ctx.layout
+        cid = _lib.COMP_IDS[ctx.comp]
+        batch = _tracks_struct(coords, wd, layout)
+        ts, gs = batch.c_struct(), layout.grid.c_struct()
+        nO, nT, nP = layout.grid.n
+        dev = coords[0].device
+        g = [(gr.detach().contiguous().to(torch.float64) if gr is not None
+              else torch.zeros((nP, nT, nO), dtype=torch.float64, device=dev))
+             for gr in grad_outs]
+        grads = [torch.empty_like(c) for c in coords]
+        gw = torch.empty(layout.n_tracks, dtype=torch.float64, device=dev)
+        need = getattr(L, f"sr_{layout.mode}_backward_workspace_bytes")(ctypes.byref(ts),
+                                                                         ctypes.byref(gs))
+        if need < 0:
+            _lib.check(_lib.SR_ERR_INVALID)
+        ws = layout.workspace.get(max(int(need), 256))
+        gptrs = (ctypes.c_void_p * 6)(*([t.data_ptr() for t in g] + [None] * (6 - len(g))))
+        tptrs = (ctypes.c_void_p * 6)(*[t.data_ptr() for t in grads])
+        stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        bwd = getattr(L, f"sr_{layout.mode}_backward")
+        _lib.check(bwd(ctypes.byref(ts), ctypes.byref(gs), cid, gptrs, saved.data_ptr(), tptrs,
+                       gw.data_ptr(), ws.data_ptr(), ctypes.c_size_t(int(need)), stream))
+        return (*grads, gw, None, None)
+
+
+def far_spectrum(x, y, z, ux, uy, uz, w, layout: SpectrumLayout, comp: str = "total"):
+    """Differentiable far-field spectrum of any comp: a tuple of its outputs
+    (device layout ``[nPhi, nTheta, nOmega]`` each, the reference's keys in
+    order: ``synchrad/calc.py:458-465``)."""
+    if layout.mode != "far":
+        raise ValueError("far_spectrum needs a far-field layout")
+    if comp not in _lib.COMP_IDS:
+        raise ValueError(f"unknown comp {comp!r}")
+    return SpectrumComps.apply(x, y, z, ux, uy, uz, w, layout, comp)
+
+
+def near_spectrum(x, y, z, ux, uy, uz, w, layout: SpectrumLayout, comp: str = "total"):
+    """Differentiable near-field (screen) spectrum of comp 'total', 'cartesian'
+    or 'cartesian_complex': a tuple of its outputs (device layout
+    ``[nPhi, nR, nOmega]`` each)."""
+    if layout.mode != "near":
+        raise ValueError("near_spectrum needs a near-field layout (mode='near')")
+    if comp not in ("total", "cartesian", "cartesian_complex"):
+        raise ValueError(f"comp {comp!r} is not a near-field comp")
+    return SpectrumComps.apply(x, y, z, ux, uy, uz, w, layout, comp)
 
 
 def far_total_spectrum(x, y, z, ux, uy, uz, w, layout: SpectrumLayout) -> torch.Tensor:

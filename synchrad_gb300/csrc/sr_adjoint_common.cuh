@@ -83,10 +83,10 @@ __global__ void adj_items_kernel(FarMixedParams p, int64_t *item_off, uint32_t s
   if (threadIdx.x == blockDim.x - 1) item_off[n] = sums[blockDim.x - 1];
 }
 
-// dL/dw_t = sum_p g(p) dt^2 |A_t(p)|^2 in two fixed-order stages: block
-// (t, b) sums chunk b of track t's points (F4 float4 of saved amplitudes per
-// point; padding floats are zero) into wpart[t][b] by a fixed tree, then one
-// thread per track adds its chunks in order.
+// Weight gradients are summed in two fixed-order stages: block (t, b) sums
+// chunk b of track t's points into wpart[t][b] by a fixed tree, then one
+// thread per track adds its chunks in order (sr_far_adjoint.cu,
+// sr_near_adjoint.cu).
 constexpr int kWeightThreads = 256;
 
 inline uint32_t adj_weight_chunks(uint64_t P, uint32_t n_tracks, int n_sm) {
@@ -95,41 +95,6 @@ inline uint32_t adj_weight_chunks(uint64_t P, uint32_t n_tracks, int n_sm) {
   if (c > cmax) c = cmax;
   if (c > 256) c = 256;
   return (uint32_t)(c < 1 ? 1 : c);
-}
-
-template <int F4>
-__global__ void adj_weight_partial_kernel(const float4 *save_A, const double *grad_spec,
-                                          uint64_t P, uint32_t n_chunks, double *wpart) {
-  const uint32_t t = blockIdx.x / n_chunks, b = blockIdx.x % n_chunks;
-  const uint64_t chunk = (P + n_chunks - 1) / n_chunks;
-  const uint64_t g0 = (uint64_t)b * chunk, g1 = min(P, g0 + chunk);
-  double acc = 0.0;
-  for (uint64_t g = g0 + threadIdx.x; g < g1; g += blockDim.x) {
-    double a2 = 0.0;
-#pragma unroll
-    for (int k = 0; k < F4; ++k) {
-      const float4 A = save_A[((uint64_t)t * P + g) * F4 + k];
-      a2 += (double)A.x * A.x + (double)A.y * A.y + (double)A.z * A.z + (double)A.w * A.w;
-    }
-    acc += grad_spec[g] * a2;
-  }
-  __shared__ double red[kWeightThreads];
-  red[threadIdx.x] = acc;
-  __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) wpart[blockIdx.x] = red[0];
-}
-
-__global__ void adj_weight_final_kernel(const double *wpart, uint32_t n_tracks,
-                                        uint32_t n_chunks, double dt, double *grad_w) {
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n_tracks) return;
-  double s = 0.0;
-  for (uint32_t b = 0; b < n_chunks; ++b) s += wpart[(uint64_t)t * n_chunks + b];
-  grad_w[t] = s * dt * dt;
 }
 
 }  // namespace

@@ -1,4 +1,4 @@
-// Adjoint of the mixed-precision far field (comp 'total', one snapshot).
+// Adjoint of the mixed-precision far field (every comp, one snapshot).
 //
 // Forward (sr_far_mixed.cu):  S(p) = sum_t w_t dt^2 |A_t(p)|^2,
 //   A_t(p) = sum_s m_s(p) amp_s(p) exp(i omega tau_s(p)),  carried on
@@ -11,6 +11,14 @@
 //   dL/dbbar_s, dL/da_s from amp(bbar, a), then bbar_s = (beta_s + beta_{s+1})/2,
 //   a_s = (beta_{s+1} - beta_s)/dt, beta = u/gamma.
 // The |dphase| < pi mask is held fixed (its decisions are the forward's).
+// The comps differ only in how the loss sees A (point sensitivity, below):
+//   quadratic comps (total, cartesian, spheric: outputs w dt^2 |b_k . A|^2
+//   with b_k the output's unit vector on (theta-hat, phi-hat)):
+//     U = w M A,  M = 2 dt^2 sum_k g_k b_k b_k^T (2 x 2, real);
+//   linear comps (cartesian_complex, spheric_complex: outputs sqrt(w) dt
+//   f(omega) Re/Im (b_k . A), f the FormFactor or 1):
+//     U = sqrt(w) V,  V = dt f sum_k (g_k,re + i g_k,im) b_k;
+// so that dL = Re(conj(U) . dA), and dL/dw_t = sum_p Re(conj(U) . A_t) / (2 w_t).
 //
 // Layout: E and F are sums over omega for each (direction, step), so a lane
 // owns one step and walks the omega axis of a direction with the rotation
@@ -40,9 +48,10 @@ constexpr int kAG = 9;                // per-step gradient components: x (3), bb
 
 struct AdjParams {
   FarMixedParams f;            // tracks, grid, records, status
-  const double *grad_spec;     // [P] dL/dS in the device layout
+  const double *grad_out[6];   // [P] dL/dS_k per output of the comp, device layout
+  int linear;                  // comp is linear in A (the *_complex comps)
   const float4 *save_A;        // [n_tracks][P] (A_th re, im, A_ph re, im)
-  float *gsf;                  // [P] 2 dt^2 dL/dS in FP32
+  float4 *gcst;                // [P] point sensitivity in FP32: M (xx, xy, yy, 0) or V
   float4 *wtab;                // [nO] (omega/2pi hi, lo, omega, |omega|) in FP32
   float4 *dirtab;              // [n_dirs][4] direction constants
   AdjGlobals *glob;
@@ -52,7 +61,60 @@ struct AdjParams {
   double *grad_w;              // [n_tracks]
 };
 
-// 2 dt^2 g(p) in FP32, and the direction table:
+// Point sensitivity of the loss to (A_theta, A_phi) for output gradients g_k
+// at point gi: M = (xx, xy, yy) of the quadratic comps (2 dt^2 included) or V
+// = (th re, th im, ph re, ph im) of the linear ones (dt and FormFactor
+// included), in FP64.
+__device__ __forceinline__ void point_sens(const AdjParams &a, uint64_t gi, double out[4]) {
+  const FarMixedParams &p = a.f;
+  const uint32_t nO = p.n_omega, nT = p.n_theta;
+  const uint64_t d = gi / nO;
+  const uint32_t m = (uint32_t)(gi - d * nO);
+  const uint32_t iT = (uint32_t)(d % nT), iP = (uint32_t)(d / nT);
+  const double sT = p.sin_theta[iT], cT = p.cos_theta[iT];
+  const double sP = p.sin_phi[iP], cP = p.cos_phi[iP];
+  // output unit vectors x, y, z on (theta-hat, phi-hat)
+  const double bt[3] = {cT * cP, cT * sP, -sT}, bp[3] = {-sP, cP, 0.0};
+  const double s2 = 2.0 * p.dt * p.dt;
+  auto g = [&](int k) { return a.grad_out[k][gi]; };
+  out[0] = out[1] = out[2] = out[3] = 0.0;
+  switch (p.comp) {
+    case SR_COMP_TOTAL:
+      out[0] = out[2] = s2 * g(0);
+      break;
+    case SR_COMP_CARTESIAN:
+      for (int k = 0; k < 3; ++k) {
+        const double gk = s2 * g(k);
+        out[0] += gk * bt[k] * bt[k];
+        out[1] += gk * bt[k] * bp[k];
+        out[2] += gk * bp[k] * bp[k];
+      }
+      break;
+    case SR_COMP_SPHERIC:  // outputs r (identically 0), theta, phi
+      out[0] = s2 * g(1);
+      out[2] = s2 * g(2);
+      break;
+    case SR_COMP_CARTESIAN_COMPLEX: {
+      const double f = p.dt * p.form_factor[m];
+      for (int k = 0; k < 3; ++k) {
+        const double gr = f * g(2 * k), gim = f * g(2 * k + 1);
+        out[0] += gr * bt[k];
+        out[1] += gim * bt[k];
+        out[2] += gr * bp[k];
+        out[3] += gim * bp[k];
+      }
+      break;
+    }
+    default:  // SR_COMP_SPHERIC_COMPLEX: rre, rim (identically 0), theta, phi re/im
+      out[0] = p.dt * g(2);
+      out[1] = p.dt * g(3);
+      out[2] = p.dt * g(4);
+      out[3] = p.dt * g(5);
+      break;
+  }
+}
+
+// Point sensitivities in FP32, and the direction table:
 //   [0] (1 - cos theta hi, lo, n_x hi, lo)   [1] (n_y hi, lo, 1 - cos theta, n_x)
 //   [2] (n_y, n_z, theta-hat x, y)           [3] (theta-hat z, phi-hat x, y, 0)
 __global__ void adj_prep_kernel(AdjParams a) {
@@ -60,10 +122,12 @@ __global__ void adj_prep_kernel(AdjParams a) {
   const uint32_t nT = p.n_theta;
   const uint64_t n_dirs = (uint64_t)nT * p.n_phi;
   const uint64_t P = n_dirs * p.n_omega;
-  const double s2 = 2.0 * p.dt * p.dt;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P; i += stride)
-    a.gsf[i] = (float)(s2 * a.grad_spec[i]);
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P; i += stride) {
+    double v[4];
+    point_sens(a, i, v);
+    a.gcst[i] = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
+  }
   for (uint64_t d = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; d < n_dirs; d += stride) {
     const uint32_t iT = (uint32_t)(d % nT), iP = (uint32_t)(d / nT);
     const double sT = p.sin_theta[iT], cT = p.cos_theta[iT];
@@ -78,6 +142,48 @@ __global__ void adj_prep_kernel(AdjParams a) {
   }
 }
 
+
+// dL/dw_t = sum_p Re(conj(U) . A_t) / (2 w_t) in two fixed-order stages:
+// block (t, b) sums chunk b of track t's points into wpart[t][b] (FP64, from
+// the FP64 point sensitivities), then one thread per track adds its chunks.
+__global__ void adj_weight_partial_far_kernel(AdjParams a, uint64_t P, uint32_t n_chunks,
+                                              double *wpart) {
+  const uint32_t t = blockIdx.x / n_chunks, b = blockIdx.x % n_chunks;
+  const uint64_t chunk = (P + n_chunks - 1) / n_chunks;
+  const uint64_t g0 = (uint64_t)b * chunk, g1 = min(P, g0 + chunk);
+  double acc = 0.0;
+  for (uint64_t g = g0 + threadIdx.x; g < g1; g += blockDim.x) {
+    double v[4];
+    point_sens(a, g, v);
+    const float4 A = a.save_A[(uint64_t)t * P + g];
+    const double ar = A.x, ai = A.y, br = A.z, bi = A.w;
+    if (a.linear)  // Re(conj(V) . A)
+      acc += v[0] * ar + v[1] * ai + v[2] * br + v[3] * bi;
+    else           // A^H M A
+      acc += v[0] * (ar * ar + ai * ai) + 2.0 * v[1] * (ar * br + ai * bi) +
+             v[2] * (br * br + bi * bi);
+  }
+  __shared__ double red[kWeightThreads];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) wpart[blockIdx.x] = red[0];
+}
+
+// quadratic comps: dL/dw = (A^H M A) / 2 (M holds 2 dt^2); linear comps:
+// dL/dw = Re(conj(V) . A) / (2 sqrt(w)).
+__global__ void adj_weight_final_far_kernel(const double *wpart, uint32_t n_tracks,
+                                            uint32_t n_chunks, int linear, const double *weight,
+                                            double *grad_w) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tracks) return;
+  double s = 0.0;
+  for (uint32_t b = 0; b < n_chunks; ++b) s += wpart[(uint64_t)t * n_chunks + b];
+  grad_w[t] = linear ? (weight[t] > 0.0 ? s / (2.0 * sqrt(weight[t])) : 0.0) : 0.5 * s;
+}
 
 // Per-step gradients: map dL/dbbar and dL/da of steps s-1 and s to dL/dbeta_s
 // and dL/du_s.
@@ -220,6 +326,7 @@ __global__ void __launch_bounds__(W * 32, 2) adj_far_kernel(AdjParams a) {
     // the end of a one-step item, the only record loaded
     const bool first = (si == 0);
     const float wt = (float)p.weight[t];
+    const float swt = (float)sqrt(p.weight[t]);
     const uint32_t it_start = p.it_start[t];
     double gD[kAG];
 #pragma unroll
@@ -244,10 +351,15 @@ __global__ void __launch_bounds__(W * 32, 2) adj_far_kernel(AdjParams a) {
         for (int e = 0; e < 2; ++e) {
           if (m + e < nO) {
             const uint64_t gi = dj * nO + m + e;
-            const float4 A = a.save_A[(uint64_t)t * P + gi];
-            const float g = a.gsf[gi] * wt;
+            const float4 C = a.gcst[gi];
             wv[e] = a.wtab[m + e];
-            u[e] = make_float4(g * A.x, g * A.y, g * A.z, g * A.w);
+            if (a.linear) {
+              u[e] = make_float4(swt * C.x, swt * C.y, swt * C.z, swt * C.w);
+            } else {
+              const float4 A = a.save_A[(uint64_t)t * P + gi];
+              u[e] = make_float4(wt * (C.x * A.x + C.y * A.z), wt * (C.x * A.y + C.y * A.w),
+                                 wt * (C.y * A.x + C.z * A.z), wt * (C.y * A.y + C.z * A.w));
+            }
             w[e] = make_float4(wv[e].z * u[e].x, -wv[e].z * u[e].y, wv[e].z * u[e].z,
                                -wv[e].z * u[e].w);
           } else {
@@ -413,7 +525,7 @@ __global__ void __launch_bounds__(W * 32, 2) adj_far_kernel(AdjParams a) {
 size_t adj_smem_bytes() { return sizeof(AdjSmem); }
 
 struct AdjLayout {
-  size_t records, gsf, wtab, dirtab, glob, item_off, gstep, wpart, total;
+  size_t records, gcst, wtab, dirtab, glob, item_off, gstep, wpart, total;
   uint32_t w_chunks;
 };
 
@@ -423,8 +535,8 @@ AdjLayout adj_layout(int64_t total_steps, uint64_t P, uint32_t n_omega, uint64_t
   AdjLayout l;
   l.w_chunks = adj_weight_chunks(P, n_tracks, device_sm_count());
   l.records = 256;
-  l.gsf = l.records + up((size_t)total_steps * kRecBytes);
-  l.wtab = l.gsf + up((size_t)P * 4);
+  l.gcst = l.records + up((size_t)total_steps * kRecBytes);
+  l.wtab = l.gcst + up((size_t)P * 16);
   l.dirtab = l.wtab + up((size_t)n_omega * 16);
   l.glob = l.dirtab + up((size_t)n_dirs * 64);
   l.item_off = l.glob + 256;
@@ -434,8 +546,9 @@ AdjLayout adj_layout(int64_t total_steps, uint64_t P, uint32_t n_omega, uint64_t
   return l;
 }
 
-int check_adjoint_args(const sr_tracks *t, const sr_grid *g, void *const *out) {
-  int rc = validate_spectrum_args(t, g, SR_COMP_TOTAL, SR_PREC_MIXED, out);
+int check_adjoint_args(const sr_tracks *t, const sr_grid *g, void *const *out,
+                       int comp = SR_COMP_TOTAL) {
+  int rc = validate_spectrum_args(t, g, comp, SR_PREC_MIXED, out);
   if (rc) return rc;
   if (g->mode != SR_MODE_FAR) return fail(SR_ERR_UNSUPPORTED, "the adjoint is far field only");
   if (t->n_snaps != 1)
@@ -448,46 +561,47 @@ int check_adjoint_args(const sr_tracks *t, const sr_grid *g, void *const *out) {
 
 using namespace sr;
 
-extern "C" int sr_far_total_forward_saved(const sr_tracks *t, const sr_grid *g, double *spectrum,
-                                          float *saved_A, void *workspace,
-                                          size_t workspace_bytes, void *stream) {
+extern "C" int sr_far_forward_saved(const sr_tracks *t, const sr_grid *g, int comp,
+                                    int precision, void *const *out, float *saved_A,
+                                    void *workspace, size_t workspace_bytes, void *stream) {
   clear_error();
-  void *out[6] = {spectrum};
-  int rc = check_adjoint_args(t, g, out);
+  int rc = check_adjoint_args(t, g, out, comp);
   if (rc) return rc;
+  if (precision != SR_PREC_MIXED && precision != SR_PREC_DF)
+    return fail(SR_ERR_INVALID, "precision %d (SR_PREC_MIXED or SR_PREC_DF)", precision);
   if (!saved_A) return fail(SR_ERR_INVALID, "saved_A is NULL");
   const uint64_t P = (uint64_t)g->n_omega * g->n_theta * g->n_phi;
   if (P == 0 || t->n_tracks == 0) return SR_OK;
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e = cudaMemsetAsync(saved_A, 0, (size_t)t->n_tracks * P * 16, s);
   if (e != cudaSuccess) return cuda_fail(e, "saved_A reset");
-  const FarMixedConfig cfg = mixed_config(t, g, SR_COMP_TOTAL);
-  FarMixedParams p = make_far_mixed_params(t, g, SR_COMP_TOTAL, out);
+  FarMixedParams p = make_far_mixed_params(t, g, comp, out);
   p.save_A = saved_A;
-  return launch_far_mixed(p, cfg, workspace, workspace_bytes, s);
+  if (precision == SR_PREC_DF) {
+    const FarMixedConfig cfg =
+        far_df_choose(g->n_omega, g->n_theta * g->n_phi, t->n_tracks, device_sm_count());
+    return launch_far_df(p, cfg, workspace, workspace_bytes, s);
+  }
+  return launch_far_mixed(p, mixed_config(t, g, comp), workspace, workspace_bytes, s);
+}
+
+extern "C" int sr_far_total_forward_saved(const sr_tracks *t, const sr_grid *g, double *spectrum,
+                                          float *saved_A, void *workspace,
+                                          size_t workspace_bytes, void *stream) {
+  void *out[6] = {spectrum};
+  return sr_far_forward_saved(t, g, SR_COMP_TOTAL, SR_PREC_MIXED, out, saved_A, workspace,
+                              workspace_bytes, stream);
 }
 
 extern "C" int sr_far_total_forward_saved_df(const sr_tracks *t, const sr_grid *g,
                                              double *spectrum, float *saved_A, void *workspace,
                                              size_t workspace_bytes, void *stream) {
-  clear_error();
   void *out[6] = {spectrum};
-  int rc = check_adjoint_args(t, g, out);
-  if (rc) return rc;
-  if (!saved_A) return fail(SR_ERR_INVALID, "saved_A is NULL");
-  const uint64_t P = (uint64_t)g->n_omega * g->n_theta * g->n_phi;
-  if (P == 0 || t->n_tracks == 0) return SR_OK;
-  cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = cudaMemsetAsync(saved_A, 0, (size_t)t->n_tracks * P * 16, s);
-  if (e != cudaSuccess) return cuda_fail(e, "saved_A reset");
-  const FarMixedConfig cfg =
-      far_df_choose(g->n_omega, g->n_theta * g->n_phi, t->n_tracks, device_sm_count());
-  FarMixedParams p = make_far_mixed_params(t, g, SR_COMP_TOTAL, out);
-  p.save_A = saved_A;
-  return launch_far_df(p, cfg, workspace, workspace_bytes, s);
+  return sr_far_forward_saved(t, g, SR_COMP_TOTAL, SR_PREC_DF, out, saved_A, workspace,
+                              workspace_bytes, stream);
 }
 
-extern "C" int64_t sr_far_total_backward_workspace_bytes(const sr_tracks *t, const sr_grid *g) {
+extern "C" int64_t sr_far_backward_workspace_bytes(const sr_tracks *t, const sr_grid *g) {
   if (!t || !g) return -1;
   const uint64_t n_dirs = (uint64_t)g->n_theta * g->n_phi;
   return (int64_t)adj_layout(t->total_steps, n_dirs * g->n_omega, g->n_omega, n_dirs,
@@ -495,13 +609,26 @@ extern "C" int64_t sr_far_total_backward_workspace_bytes(const sr_tracks *t, con
       .total;
 }
 
+extern "C" int64_t sr_far_total_backward_workspace_bytes(const sr_tracks *t, const sr_grid *g) {
+  return sr_far_backward_workspace_bytes(t, g);
+}
+
 extern "C" int sr_far_total_backward(const sr_tracks *t, const sr_grid *g,
                                      const double *grad_spectrum, const float *saved_A,
                                      double *const *grad_track, double *grad_weight,
                                      void *workspace, size_t workspace_bytes, void *stream) {
+  const double *grad_out[6] = {grad_spectrum};
+  return sr_far_backward(t, g, SR_COMP_TOTAL, grad_out, saved_A, grad_track, grad_weight,
+                         workspace, workspace_bytes, stream);
+}
+
+extern "C" int sr_far_backward(const sr_tracks *t, const sr_grid *g, int comp,
+                               const double *const *grad_out, const float *saved_A,
+                               double *const *grad_track, double *grad_weight, void *workspace,
+                               size_t workspace_bytes, void *stream) {
   clear_error();
-  void *dummy[6] = {(void *)grad_spectrum};
-  int rc = check_adjoint_args(t, g, dummy);
+  if (!grad_out) return fail(SR_ERR_INVALID, "grad_out must not be NULL");
+  int rc = check_adjoint_args(t, g, (void *const *)grad_out, comp);
   if (rc) return rc;
   if (!saved_A || !grad_track || !grad_weight)
     return fail(SR_ERR_INVALID, "saved_A, grad_track and grad_weight must not be NULL");
@@ -530,12 +657,13 @@ extern "C" int sr_far_total_backward(const sr_tracks *t, const sr_grid *g,
 
   AdjParams a;
   memset(&a, 0, sizeof(a));
-  a.f = make_far_mixed_params(t, g, SR_COMP_TOTAL, dummy);
+  a.f = make_far_mixed_params(t, g, comp, (void *const *)grad_out);
   a.f.status = (int *)w;
   a.f.records = (float4 *)(w + lay.records);
-  a.grad_spec = grad_spectrum;
+  for (int i = 0; i < n_outputs(comp); ++i) a.grad_out[i] = grad_out[i];
+  a.linear = (comp == SR_COMP_CARTESIAN_COMPLEX || comp == SR_COMP_SPHERIC_COMPLEX) ? 1 : 0;
   a.save_A = (const float4 *)saved_A;
-  a.gsf = (float *)(w + lay.gsf);
+  a.gcst = (float4 *)(w + lay.gcst);
   a.wtab = (float4 *)(w + lay.wtab);
   a.dirtab = (float4 *)(w + lay.dirtab);
   a.glob = (AdjGlobals *)(w + lay.glob);
@@ -559,10 +687,10 @@ extern "C" int sr_far_total_backward(const sr_tracks *t, const sr_grid *g,
   adj_items_kernel<<<1, 1024, 0, s>>>(a.f, a.item_off, (uint32_t)kASteps);
   {
     double *wpart = (double *)(w + lay.wpart);
-    adj_weight_partial_kernel<1><<<t->n_tracks * lay.w_chunks, kWeightThreads, 0, s>>>(
-        a.save_A, grad_spectrum, P, lay.w_chunks, wpart);
-    adj_weight_final_kernel<<<(t->n_tracks + 255) / 256, 256, 0, s>>>(
-        wpart, t->n_tracks, lay.w_chunks, t->dt, grad_weight);
+    adj_weight_partial_far_kernel<<<t->n_tracks * lay.w_chunks, kWeightThreads, 0, s>>>(
+        a, P, lay.w_chunks, wpart);
+    adj_weight_final_far_kernel<<<(t->n_tracks + 255) / 256, 256, 0, s>>>(
+        wpart, t->n_tracks, lay.w_chunks, a.linear, t->weight, grad_weight);
   }
   rc = cuda_fail(cudaGetLastError(), "adjoint prep launch");
   if (rc) return rc;

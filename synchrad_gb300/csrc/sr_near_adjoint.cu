@@ -1,4 +1,4 @@
-// Adjoint of the mixed-precision near field (comp 'total', one snapshot).
+// Adjoint of the mixed-precision near field (every comp, one snapshot).
 //
 // Forward (sr_near_mixed.cu, the reference's synchrad/kernel_nearfield.cl:58-102):
 //   S(p) = sum_t w_t dt^2 |A_t(p)|^2,   A = sum_s a_s e^{i phi_s},
@@ -12,7 +12,12 @@
 // per step and screen point, with the omega sums (per component k)
 //   R0_k = sum Re(U_k z),  I1_k = sum omega Im(U_k z),  R2_k = sum omega^2 Re(U_k z)
 // (from d phi/dx = -omega n, dn/dx = -(I - n n^T)/r, dr/dx = -n), then
-// dL/du = dL/dbeta / gamma - u (u . dL/dbeta) / gamma^3.  beta - n is formed
+// dL/du = dL/dbeta / gamma - u (u . dL/dbeta) / gamma^3.  The comps differ in
+// U_k only: total and cartesian (outputs w dt^2 |A_k|^2 summed or apart) give
+// U_k = 2 g_k w dt^2 A_k (g_k = g for total); cartesian_complex (outputs sqrt(w)
+// dt Re/Im(e^{i omega L} A_k)) gives U_k = sqrt(w) dt (g_k,re + i g_k,im)
+// e^{-i omega L}; with dL = Re(conj(U) . dA), dL/dw = sum_p Re(conj(U) . A)/(2w).
+// beta - n is formed
 // as in the forward ((1 - n_z) - (1 - beta_z) along z).  The |dphase| < pi
 // mask is held fixed (its decisions are the forward's).
 //
@@ -43,9 +48,12 @@ constexpr int kNAPair = 11;           // float4 per pair of slots in the constan
 
 struct NearAdjParams {
   FarMixedParams f;            // tracks, grid (n_theta = radii), records, status
-  const double *grad_spec;     // [P] dL/dS in the device layout
+  const double *grad_out[6];   // [P] dL/dS_k per output of the comp, device layout
+  int linear;                  // cartesian_complex: U does not depend on A
   const float4 *save_A;        // [n_tracks][P][2] (A_x re, im, A_y re, im), (A_z re, im, 0, 0)
-  float *gsf;                  // [P] 2 dt^2 dL/dS in FP32
+  float4 *gcst;                // [P][2] point sensitivity in FP32: quadratic comps
+                               // (2 dt^2 g_x, g_y, g_z, 0), 0; linear (V_x re, im,
+                               // V_y re, im), (V_z re, im, 0, 0)
   float4 *wtab;                // [nO] (omega/2pi hi, lo, omega, |omega|) in FP32
   float4 *sctab;               // [n_screen] (X hi, lo, Y hi, lo) of the screen point
   AdjGlobals *glob;
@@ -55,16 +63,81 @@ struct NearAdjParams {
   double *grad_w;              // [n_tracks]
 };
 
-// 2 dt^2 g(p) in FP32 and the screen table.
+// Point sensitivity (FP64) of the loss to (A_x, A_y, A_z) at point gi for the
+// output gradients g_k: quadratic comps 2 dt^2 (g_x, g_y, g_z) in v[0..2];
+// cartesian_complex V_k = dt (g_k,re + i g_k,im) e^{-i omega L} in v[0..5].
+__device__ __forceinline__ void near_point_sens(const NearAdjParams &a, uint64_t gi,
+                                                double v[6]) {
+  const FarMixedParams &p = a.f;
+  const double s2 = 2.0 * p.dt * p.dt;
+  for (int k = 0; k < 6; ++k) v[k] = 0.0;
+  if (p.comp == SR_COMP_TOTAL) {
+    v[0] = v[1] = v[2] = s2 * a.grad_out[0][gi];
+  } else if (p.comp == SR_COMP_CARTESIAN) {
+    for (int k = 0; k < 3; ++k) v[k] = s2 * a.grad_out[k][gi];
+  } else {  // cartesian_complex (FormFactor not applied, as the reference)
+    const double w = p.omega[gi % p.n_omega];
+    double sL, cL;
+    sincos(w * p.L_screen, &sL, &cL);
+    for (int k = 0; k < 3; ++k) {
+      const double gr = a.grad_out[2 * k][gi], gim = a.grad_out[2 * k + 1][gi];
+      v[2 * k] = p.dt * (gr * cL + gim * sL);
+      v[2 * k + 1] = p.dt * (gim * cL - gr * sL);
+    }
+  }
+}
+
+// dL/dw_t = sum_p Re(conj(U) . A_t) / (2 w_t): chunk sums in FP64 from the
+// FP64 point sensitivities, then one thread per track adds its chunks.
+__global__ void nadj_weight_partial_kernel(NearAdjParams a, uint64_t P, uint32_t n_chunks,
+                                           double *wpart) {
+  const uint32_t t = blockIdx.x / n_chunks, b = blockIdx.x % n_chunks;
+  const uint64_t chunk = (P + n_chunks - 1) / n_chunks;
+  const uint64_t g0 = (uint64_t)b * chunk, g1 = min(P, g0 + chunk);
+  double acc = 0.0;
+  for (uint64_t g = g0 + threadIdx.x; g < g1; g += blockDim.x) {
+    double v[6];
+    near_point_sens(a, g, v);
+    const float4 A0 = a.save_A[2 * ((uint64_t)t * P + g)];
+    const float4 A1 = a.save_A[2 * ((uint64_t)t * P + g) + 1];
+    const double re[3] = {A0.x, A0.z, A1.x}, im[3] = {A0.y, A0.w, A1.y};
+    for (int k = 0; k < 3; ++k)
+      acc += a.linear ? v[2 * k] * re[k] + v[2 * k + 1] * im[k]
+                      : v[k] * (re[k] * re[k] + im[k] * im[k]);
+  }
+  __shared__ double red[kWeightThreads];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) wpart[blockIdx.x] = red[0];
+}
+
+__global__ void nadj_weight_final_kernel(const double *wpart, uint32_t n_tracks,
+                                         uint32_t n_chunks, int linear, const double *weight,
+                                         double *grad_w) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tracks) return;
+  double s = 0.0;
+  for (uint32_t b = 0; b < n_chunks; ++b) s += wpart[(uint64_t)t * n_chunks + b];
+  grad_w[t] = linear ? (weight[t] > 0.0 ? s / (2.0 * sqrt(weight[t])) : 0.0) : 0.5 * s;
+}
+
+// Point sensitivities in FP32 and the screen table.
 __global__ void nadj_prep_kernel(NearAdjParams a) {
   const FarMixedParams &p = a.f;
   const uint32_t nR = p.n_theta;
   const uint64_t n_scr = (uint64_t)nR * p.n_phi;
   const uint64_t P = n_scr * p.n_omega;
-  const double s2 = 2.0 * p.dt * p.dt;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P; i += stride)
-    a.gsf[i] = (float)(s2 * a.grad_spec[i]);
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P; i += stride) {
+    double v[6];
+    near_point_sens(a, i, v);
+    a.gcst[2 * i] = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
+    a.gcst[2 * i + 1] = make_float4((float)v[4], (float)v[5], 0.f, 0.f);
+  }
   for (uint64_t d = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; d < n_scr; d += stride) {
     const uint32_t iR = (uint32_t)(d % nR), iP = (uint32_t)(d / nR);
     const df X = df_from_double(p.sin_theta[iR] * p.cos_phi[iP]);  // radius * cos(phi)
@@ -226,6 +299,7 @@ __global__ void __launch_bounds__(W * 32, 2) nadj_kernel(NearAdjParams a) {
     // the end of a one-step item, the only record loaded
     const bool first = (si == 0);
     const float wt = (float)p.weight[t];
+    const float swt = (float)sqrt(p.weight[t]);
     const uint32_t it_start = p.it_start[t];
     double gD[kNAG];
 #pragma unroll
@@ -247,7 +321,7 @@ __global__ void __launch_bounds__(W * 32, 2) nadj_kernel(NearAdjParams a) {
         const uint64_t f = f0 + 2 * j;
         const uint64_t dj = f / nOp;
         const uint32_t m = (uint32_t)(f - dj * nOp);
-        float ar[2][3], ai[2][3], g[2], om[2];
+        float ar[2][3], ai[2][3], om[2];
         float4 wv[2];
 #pragma unroll
         for (int e = 0; e < 2; ++e) {
@@ -255,15 +329,20 @@ __global__ void __launch_bounds__(W * 32, 2) nadj_kernel(NearAdjParams a) {
             const uint64_t gi = dj * nO + m + e;
             const float4 A0 = a.save_A[2 * ((uint64_t)t * P + gi)];
             const float4 A1 = a.save_A[2 * ((uint64_t)t * P + gi) + 1];
-            ar[e][0] = A0.x; ai[e][0] = A0.y;
-            ar[e][1] = A0.z; ai[e][1] = A0.w;
-            ar[e][2] = A1.x; ai[e][2] = A1.y;
-            g[e] = a.gsf[gi] * wt;
+            const float4 C0 = a.gcst[2 * gi], C1 = a.gcst[2 * gi + 1];
+            if (a.linear) {  // U_k = sqrt(w) V_k
+              ar[e][0] = swt * C0.x; ai[e][0] = swt * C0.y;
+              ar[e][1] = swt * C0.z; ai[e][1] = swt * C0.w;
+              ar[e][2] = swt * C1.x; ai[e][2] = swt * C1.y;
+            } else {         // U_k = w g'_k A_k
+              ar[e][0] = wt * C0.x * A0.x; ai[e][0] = wt * C0.x * A0.y;
+              ar[e][1] = wt * C0.y * A0.z; ai[e][1] = wt * C0.y * A0.w;
+              ar[e][2] = wt * C0.z * A1.x; ai[e][2] = wt * C0.z * A1.y;
+            }
             wv[e] = a.wtab[m + e];
           } else {
 #pragma unroll
             for (int k = 0; k < 3; ++k) ar[e][k] = ai[e][k] = 0.f;
-            g[e] = 0.f;
             wv[e] = make_float4(0.f, 0.f, 0.f, 0.f);
           }
           om[e] = wv[e].z;
@@ -271,8 +350,8 @@ __global__ void __launch_bounds__(W * 32, 2) nadj_kernel(NearAdjParams a) {
         float4 *o = sm.cst[j];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-          const float u0r = g[0] * ar[0][k], u1r = g[1] * ar[1][k];
-          const float u0i = g[0] * ai[0][k], u1i = g[1] * ai[1][k];
+          const float u0r = ar[0][k], u1r = ar[1][k];
+          const float u0i = ai[0][k], u1i = ai[1][k];
           o[k] = make_float4(u0r, u1r, u0i, u1i);
           o[3 + k] = make_float4(om[0] * u0r, om[1] * u1r, -om[0] * u0i, -om[1] * u1i);
           o[6 + k] = make_float4(om[0] * om[0] * u0r, om[1] * om[1] * u1r, om[0] * om[0] * u0i,
@@ -425,7 +504,7 @@ __global__ void __launch_bounds__(W * 32, 2) nadj_kernel(NearAdjParams a) {
 size_t nadj_smem_bytes() { return sizeof(NearAdjSmem); }
 
 struct NearAdjLayout {
-  size_t records, gsf, wtab, sctab, glob, item_off, gstep, wpart, total;
+  size_t records, gcst, wtab, sctab, glob, item_off, gstep, wpart, total;
   uint32_t w_chunks;
 };
 
@@ -435,8 +514,8 @@ NearAdjLayout nadj_layout(int64_t total_steps, uint64_t P, uint32_t n_omega, uin
   NearAdjLayout l;
   l.w_chunks = adj_weight_chunks(P, n_tracks, device_sm_count());
   l.records = 256;
-  l.gsf = l.records + up((size_t)total_steps * kRecBytes);
-  l.wtab = l.gsf + up((size_t)P * 4);
+  l.gcst = l.records + up((size_t)total_steps * kRecBytes);
+  l.wtab = l.gcst + up((size_t)P * 32);
   l.sctab = l.wtab + up((size_t)n_omega * 16);
   l.glob = l.sctab + up((size_t)n_scr * 16);
   l.item_off = l.glob + 256;
@@ -446,8 +525,9 @@ NearAdjLayout nadj_layout(int64_t total_steps, uint64_t P, uint32_t n_omega, uin
   return l;
 }
 
-int check_near_adjoint_args(const sr_tracks *t, const sr_grid *g, void *const *out) {
-  int rc = validate_spectrum_args(t, g, SR_COMP_TOTAL, SR_PREC_MIXED, out);
+int check_near_adjoint_args(const sr_tracks *t, const sr_grid *g, void *const *out,
+                            int comp = SR_COMP_TOTAL) {
+  int rc = validate_spectrum_args(t, g, comp, SR_PREC_MIXED, out);
   if (rc) return rc;
   if (g->mode != SR_MODE_NEAR) return fail(SR_ERR_UNSUPPORTED, "near-field adjoint: mode near");
   if (t->n_snaps != 1)
@@ -460,12 +540,11 @@ int check_near_adjoint_args(const sr_tracks *t, const sr_grid *g, void *const *o
 
 using namespace sr;
 
-extern "C" int sr_near_total_forward_saved(const sr_tracks *t, const sr_grid *g, double *spectrum,
-                                           float *saved_A, void *workspace,
-                                           size_t workspace_bytes, void *stream) {
+extern "C" int sr_near_forward_saved(const sr_tracks *t, const sr_grid *g, int comp,
+                                     void *const *out, float *saved_A, void *workspace,
+                                     size_t workspace_bytes, void *stream) {
   clear_error();
-  void *out[6] = {spectrum};
-  int rc = check_near_adjoint_args(t, g, out);
+  int rc = check_near_adjoint_args(t, g, out, comp);
   if (rc) return rc;
   if (!saved_A) return fail(SR_ERR_INVALID, "saved_A is NULL");
   const uint64_t P = (uint64_t)g->n_omega * g->n_theta * g->n_phi;
@@ -473,13 +552,24 @@ extern "C" int sr_near_total_forward_saved(const sr_tracks *t, const sr_grid *g,
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e = cudaMemsetAsync(saved_A, 0, (size_t)t->n_tracks * P * 32, s);
   if (e != cudaSuccess) return cuda_fail(e, "saved_A reset");
-  const FarMixedConfig cfg = mixed_config(t, g, SR_COMP_TOTAL);
-  FarMixedParams p = make_far_mixed_params(t, g, SR_COMP_TOTAL, out);
+  FarMixedParams p = make_far_mixed_params(t, g, comp, out);
   p.save_A = saved_A;
-  return launch_near_mixed(p, cfg, workspace, workspace_bytes, s);
+  return launch_near_mixed(p, mixed_config(t, g, comp), workspace, workspace_bytes, s);
+}
+
+extern "C" int sr_near_total_forward_saved(const sr_tracks *t, const sr_grid *g, double *spectrum,
+                                           float *saved_A, void *workspace,
+                                           size_t workspace_bytes, void *stream) {
+  void *out[6] = {spectrum};
+  return sr_near_forward_saved(t, g, SR_COMP_TOTAL, out, saved_A, workspace, workspace_bytes,
+                               stream);
 }
 
 extern "C" int64_t sr_near_total_backward_workspace_bytes(const sr_tracks *t, const sr_grid *g) {
+  return sr_near_backward_workspace_bytes(t, g);
+}
+
+extern "C" int64_t sr_near_backward_workspace_bytes(const sr_tracks *t, const sr_grid *g) {
   if (!t || !g) return -1;
   const uint64_t n_scr = (uint64_t)g->n_theta * g->n_phi;
   return (int64_t)nadj_layout(t->total_steps, n_scr * g->n_omega, g->n_omega, n_scr,
@@ -491,9 +581,18 @@ extern "C" int sr_near_total_backward(const sr_tracks *t, const sr_grid *g,
                                       const double *grad_spectrum, const float *saved_A,
                                       double *const *grad_track, double *grad_weight,
                                       void *workspace, size_t workspace_bytes, void *stream) {
+  const double *grad_out[6] = {grad_spectrum};
+  return sr_near_backward(t, g, SR_COMP_TOTAL, grad_out, saved_A, grad_track, grad_weight,
+                          workspace, workspace_bytes, stream);
+}
+
+extern "C" int sr_near_backward(const sr_tracks *t, const sr_grid *g, int comp,
+                                const double *const *grad_out, const float *saved_A,
+                                double *const *grad_track, double *grad_weight, void *workspace,
+                                size_t workspace_bytes, void *stream) {
   clear_error();
-  void *dummy[6] = {(void *)grad_spectrum};
-  int rc = check_near_adjoint_args(t, g, dummy);
+  if (!grad_out) return fail(SR_ERR_INVALID, "grad_out must not be NULL");
+  int rc = check_near_adjoint_args(t, g, (void *const *)grad_out, comp);
   if (rc) return rc;
   if (!saved_A || !grad_track || !grad_weight)
     return fail(SR_ERR_INVALID, "saved_A, grad_track and grad_weight must not be NULL");
@@ -522,12 +621,13 @@ extern "C" int sr_near_total_backward(const sr_tracks *t, const sr_grid *g,
 
   NearAdjParams a;
   memset(&a, 0, sizeof(a));
-  a.f = make_far_mixed_params(t, g, SR_COMP_TOTAL, dummy);
+  a.f = make_far_mixed_params(t, g, comp, (void *const *)grad_out);
   a.f.status = (int *)w;
   a.f.records = (float4 *)(w + lay.records);
-  a.grad_spec = grad_spectrum;
+  for (int i = 0; i < n_outputs(comp); ++i) a.grad_out[i] = grad_out[i];
+  a.linear = comp == SR_COMP_CARTESIAN_COMPLEX ? 1 : 0;
   a.save_A = (const float4 *)saved_A;
-  a.gsf = (float *)(w + lay.gsf);
+  a.gcst = (float4 *)(w + lay.gcst);
   a.wtab = (float4 *)(w + lay.wtab);
   a.sctab = (float4 *)(w + lay.sctab);
   a.glob = (AdjGlobals *)(w + lay.glob);
@@ -551,10 +651,10 @@ extern "C" int sr_near_total_backward(const sr_tracks *t, const sr_grid *g,
   adj_items_kernel<<<1, 1024, 0, s>>>(a.f, a.item_off, (uint32_t)kNASteps);
   {
     double *wpart = (double *)(w + lay.wpart);
-    adj_weight_partial_kernel<2><<<t->n_tracks * lay.w_chunks, kWeightThreads, 0, s>>>(
-        a.save_A, grad_spectrum, P, lay.w_chunks, wpart);
-    adj_weight_final_kernel<<<(t->n_tracks + 255) / 256, 256, 0, s>>>(
-        wpart, t->n_tracks, lay.w_chunks, t->dt, grad_weight);
+    nadj_weight_partial_kernel<<<t->n_tracks * lay.w_chunks, kWeightThreads, 0, s>>>(
+        a, P, lay.w_chunks, wpart);
+    nadj_weight_final_kernel<<<(t->n_tracks + 255) / 256, 256, 0, s>>>(
+        wpart, t->n_tracks, lay.w_chunks, a.linear, t->weight, grad_weight);
   }
   rc = cuda_fail(cudaGetLastError(), "near adjoint prep launch");
   if (rc) return rc;

@@ -62,14 +62,19 @@ def far_total_torch(x, y, z, ux, uy, uz, w, offsets, dt, omega, sinT, cosT, sinP
 
 
 def far_comps_torch(x, y, z, ux, uy, uz, w, offsets, dt, omega, sinT, cosT, sinP, cosP,
-                    comp="cartesian"):
-    """Per-component spectra [3][nPhi, nTheta, nOmega]: 'cartesian' |A_x|^2,
+                    comp="cartesian", form_factor=None):
+    """Per-component spectra [n_out][nPhi, nTheta, nOmega]: 'cartesian' |A_x|^2,
     |A_y|^2, |A_z|^2 (synchrad/kernel_farfield.cl:166-223) or 'spheric'
     |A_r|^2, |A_theta|^2, |A_phi|^2 on r = n, theta-hat = (cos theta cos phi,
     cos theta sin phi, -sin theta), phi-hat = (-sin phi, cos phi, 0)
-    (:382-388, 442-445), each times w dt^2 and summed over tracks."""
+    (:382-388, 442-445), each times w dt^2 and summed over tracks; the
+    coherent 'cartesian_complex' (times the FormFactor, :283-324) and
+    'spheric_complex' (:548-593) give Re and Im of each component times
+    sqrt(w) dt, summed over tracks (6 outputs: re, im per component)."""
     n0, n1, n2 = directions(sinT, cosT, sinP, cosP)
     N = torch.stack([n0, n1, n2], -1)
+    coherent = comp.endswith("_complex")
+    comp = comp[:-len("_complex")] if coherent else comp
     if comp == "cartesian":
         basis = torch.eye(3, dtype=torch.float64, device=x.device)[None].expand(N.shape[0], 3, 3)
     elif comp == "spheric":
@@ -82,9 +87,19 @@ def far_comps_torch(x, y, z, ux, uy, uz, w, offsets, dt, omega, sinT, cosT, sinP
         basis = torch.stack([N, th, ph], 1)  # [nDir, comp, xyz]
     else:
         raise ValueError(comp)
-    S = torch.zeros(3, N.shape[0], omega.numel(), dtype=torch.float64, device=x.device)
+    n_out = 6 if coherent else 3
+    S = torch.zeros(n_out, N.shape[0], omega.numel(), dtype=torch.float64, device=x.device)
+    ff = None
+    if coherent and comp == "cartesian" and form_factor is not None:
+        ff = form_factor[None, None, :]
     for t, re, im in _far_track_sums(x, y, z, ux, uy, uz, offsets, dt, omega, N, n0, n1, n2):
         pr = torch.einsum("dok,dck->cdo", re, basis)
         pi = torch.einsum("dok,dck->cdo", im, basis)
-        S = S + w[t] * dt * dt * (pr * pr + pi * pi)
-    return S.reshape(3, sinP.numel(), sinT.numel(), omega.numel())
+        if coherent:
+            f = torch.sqrt(w[t]) * dt
+            if ff is not None:
+                pr, pi = pr * ff, pi * ff
+            S = S + f * torch.stack([pr, pi], 1).reshape(6, N.shape[0], omega.numel())
+        else:
+            S = S + w[t] * dt * dt * (pr * pr + pi * pi)
+    return S.reshape(n_out, sinP.numel(), sinT.numel(), omega.numel())

@@ -71,3 +71,17 @@ def near_cartesian_torch(x, y, z, ux, uy, uz, w, offsets, dt, omega, radius, sin
                                       L_screen):
         S = S + w[t] * dt * dt * (re * re + im * im).permute(2, 0, 1)
     return S.reshape(3, sinP.numel(), radius.numel(), omega.numel())
+
+
+def near_cartesian_complex_torch(x, y, z, ux, uy, uz, w, offsets, dt, omega, radius, sinP,
+                                 cosP, L_screen):
+    """The coherent components [6][nPhi, nR, nOmega]: sqrt(w) dt Re A_x, Im A_x,
+    Re A_y, ..., Im A_z summed over tracks (synchrad/kernel_nearfield.cl:216-326;
+    no FormFactor)."""
+    X0, Y0 = _screen(radius, sinP, cosP)
+    D, O = X0.numel(), omega.numel()
+    S = torch.zeros(6, D, O, dtype=torch.float64, device=x.device)
+    for t, re, im in _near_track_sums(x, y, z, ux, uy, uz, offsets, dt, omega, X0, Y0,
+                                      L_screen):
+        S = S + torch.sqrt(w[t]) * dt * torch.stack([re, im], -1).permute(2, 3, 0, 1).reshape(6, D, O)
+    return S.reshape(6, sinP.numel(), radius.numel(), omega.numel())

@@ -13,7 +13,9 @@ both to 1e-6 relative L2.  The end-to-end gradient with the mixed forward is
 reported and bounded at 1e-3: S - T is about 1e-3 of S, so the mixed
 spectrum's ~1e-7 error enters dL/dS amplified.
 
-The finite differences re-evaluate only the touched track, in FP64, with the
+Steps: 1e-9 in z and 1e-7 in x, y (about 1e-3 rad of phase at omega ~ 7e5),
+1e-5 relative in the momenta.  The finite differences re-evaluate only the
+touched track, in FP64, with the
 plain FP64 CUDA kernel (the reference kernel's operations in order; equal to
 the CPU oracle to 1e-12 on every golden case): L(h) = sum(((S - S_t + S_t(h)
 - T) / max T)^2), S and T over all tracks also in FP64.
@@ -99,7 +101,9 @@ def test_misfit_gradient_at_full_size():
         s = int(rng.integers(lengths[t] - 1 if c < 3 else lengths[t]))
         base = tracks[t]
         v = base[c][s]
-        h = 1e-5 * (max(1.0, abs(v)) if c >= 3 else 1.0)
+        # steps of about 1e-3 rad in the phase at the largest omega:
+        # d(tau)/dz ~ 1, d(tau)/dx,y ~ sin(theta) <= 1.5/gamma
+        h = 1e-9 if c == 2 else (1e-7 if c < 2 else 1e-5 * max(1.0, abs(v)))
         own = fp64_spectrum([list(base)])
         others = total - own
 
