@@ -95,3 +95,49 @@ def test_near_component_spectra_match_oracle():
         exp = exp + np.stack(spec)
     for c in range(3):
         assert rel_l2(S[c], exp[c]) <= 1e-12, c
+
+
+@pytest.mark.parametrize("comp", ["cartesian_complex", "spheric_complex"])
+def test_coherent_far_components_match_oracle(comp):
+    """The coherent comps of the restatement (FormFactor on cartesian_complex
+    only, as the reference applies it) against the oracle."""
+    tracks, dt, axes, n, _ = make_case(True)
+    ff = np.exp(-0.5 * (axes[0] / float(axes[0].max())) ** 2)
+    _, offsets, coords, weights = concat(tracks)
+    ax = [torch.tensor(a, dtype=torch.float64) for a in axes]
+    S = ftr.far_comps_torch(*[torch.tensor(c) for c in coords], torch.tensor(weights), offsets,
+                            dt, *ax, comp=comp, form_factor=torch.tensor(ff)).numpy()
+    exp = 0
+    for t in tracks:
+        nst = t[0].size
+        spec = [np.zeros((n[2], n[1], n[0])) for _ in range(6)]
+        oracle.run_track("port", "far", comp, spec, [np.ascontiguousarray(a) for a in t[:6]],
+                         t[6], 0, nst, nst, axes, n, dt, np.array([nst], dtype=np.uint32),
+                         form_factor=ff, nthreads=4)
+        exp = exp + np.stack(spec)
+    scale = np.abs(exp).max()
+    for k in range(6):
+        if comp == "spheric_complex" and k < 2:  # radial: rounding noise in both
+            assert np.abs(S[k]).max() < 1e-12 * scale and np.abs(exp[k]).max() < 1e-12 * scale
+        else:
+            assert rel_l2(S[k], exp[k]) <= 1e-12, (comp, k)
+
+
+def test_coherent_near_components_match_oracle():
+    import near_torch_ref as ntr
+    from test_near_adjoint import concat as nconcat, make_case as nmake_case
+    tracks, dt, axes, n, _, L, _ = nmake_case(True, seed=8)
+    _, offsets, coords, weights = nconcat(tracks)
+    S = ntr.near_cartesian_complex_torch(*[torch.tensor(c) for c in coords],
+                                         torch.tensor(weights), offsets, dt,
+                                         *[torch.tensor(a) for a in axes], L).numpy()
+    exp = 0
+    for t in tracks:
+        nst = t[0].size
+        spec = [np.zeros((n[2], n[1], n[0])) for _ in range(6)]
+        oracle.run_track("port", "near", "cartesian_complex", spec,
+                         [np.ascontiguousarray(a) for a in t[:6]], t[6], 0, nst, nst, axes, n,
+                         dt, np.array([nst], dtype=np.uint32), L_screen=L, nthreads=4)
+        exp = exp + np.stack(spec)
+    for k in range(6):
+        assert rel_l2(S[k], exp[k]) <= 1e-11, k

@@ -5,7 +5,8 @@
 For L = sum_k sum_p g_k(p) S_k(p) with seeded weights g_k the CUDA adjoint is
 compared with autograd of the float64 PyTorch restatement (3e-6 relative L2
 per group of positions, momenta and weights) and with fourth-order central
-finite differences of the FP64 oracle on 16 coordinates (1e-6).  The coherent
+finite differences of the FP64 oracle on 16 coordinates (2e-6: the adjoint
+kernel's FP32 omega sums).  The coherent
 comp carries the phase of the screen distance, e^{i omega L}, and its weight
 gradient follows sqrt(w).
 """
@@ -22,7 +23,7 @@ from test_near_adjoint import concat, make_case  # noqa: E402
 
 COMPS = ["cartesian", "cartesian_complex"]
 TOL_AUTOGRAD = 3e-6
-TOL_FD = 1e-6
+TOL_FD = 2e-6  # as for the far comps: FP32 omega sums in the adjoint kernel
 
 
 def _case(comp):
