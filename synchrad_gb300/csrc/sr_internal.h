@@ -93,6 +93,7 @@ FarMixedConfig near_mixed_make(uint32_t n_omega, uint32_t n_screen, uint32_t n_t
 FarMixedConfig mixed_config(const sr_tracks *t, const sr_grid *g, int comp);
 FarMixedConfig far_mixed_choose(uint32_t n_omega, uint32_t n_dirs,
                                 uint32_t n_tracks, int n_sm);
+size_t far_mixed_smem_bytes(int dpw, int stage);
 size_t far_mixed_workspace(int64_t total_steps, uint64_t n_points, int n_out,
                            uint32_t n_snaps, const FarMixedConfig &cfg);
 int launch_far_mixed(FarMixedParams p, const FarMixedConfig &cfg,

@@ -8,6 +8,7 @@ namespace sr {
 namespace {
 
 constexpr int kStage = 128;         // steps per TMA stage
+constexpr size_t kMaxSmemPerCta = 232448;  // opt-in shared memory per CTA (227 KB)
 constexpr int kFoldStages = 8;      // FP32 sums fold into compensated pairs every 1024 steps
 // float4 per step record: 64 bytes of data and 16 of padding, so that 32
 // lanes reading one record each from shared memory hit every bank once per

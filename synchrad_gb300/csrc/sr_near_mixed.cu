@@ -93,8 +93,14 @@ struct NearSmemFixed {
   uint64_t bar[2];
   uint64_t pad_[2];
   ScreenConst sc[W][kNMaxDpw];
-  // followed by float4 setup[W][dpw][kNSetupF4][32]
+  float2 w0rev[W][32];  // each lane's first frequency in revolutions (double-float)
+  // followed by float4 setup[W][dpw][kNSetupF4][32] and
+  // float2 seeds[W][dpw][32 steps][L + 1]: e^{i omega_0 tau} of every lane and step
 };
+
+// float2 per warp in the seed table: dpw directions x 32 steps x (L + 1) (one
+// float2 of padding per row keeps the setup's stores free of bank conflicts)
+__host__ __device__ constexpr int near_seed_f2(int dpw) { return dpw * 32 * (32 / dpw + 1); }
 
 // Packed accumulators of one lane: six complex sums for K points.
 template <int K>
@@ -127,6 +133,8 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int dsub = lane / L, ll = lane % L;
   float4 *setup = setup_all + (size_t)warp * 32 * dpw * kNSetupF4;
+  float2 *seeds = reinterpret_cast<float2 *>(setup_all + (size_t)W * 32 * dpw * kNSetupF4) +
+                  (size_t)warp * near_seed_f2(dpw);
 
   if (threadIdx.x == 0) {
     mbar_init(&sm.bar[0], 1);
@@ -169,7 +177,10 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
       c.tprev_h = 0.f; c.tprev_l = 0.f;
     }
     const double w0d = nv > 0 ? p.omega[j0] : 0.0;
-    const df d_w0 = df_from_double(w0d * inv2pi);
+    {
+      const df d_w0 = df_from_double(w0d * inv2pi);
+      sm.w0rev[warp][lane] = make_float2(d_w0.hi, d_w0.lo);
+    }
     const float w0f = (float)w0d, dwf = (float)dw_glob;
     bool uniform = true;
     float wabs_min = 3.0e38f, wabs_max = 0.f;
@@ -290,12 +301,13 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
         }
       };
 
-      // The first pair's phasors of one step: the reseed e^{i omega_0 tau} and
-      // its product with R = e^{i d_omega tau}.
-      auto step_seed = [&](const float4 *st, float2 &ZrA, float2 &ZiA) {
+      // The first pair's phasors of step i of the chunk: the reseed
+      // e^{i omega_0 tau} (from the setup's seed table) and its product with
+      // R = e^{i d_omega tau}.
+      auto step_seed = [&](const float4 *st, uint32_t i, float2 &ZrA, float2 &ZiA) {
         const float4 A = st[0];
-        float zs, zc;
-        phasor_rev(d_w0.hi, d_w0.lo, A.x, A.y, zs, zc);
+        const float2 z0 = seeds[((size_t)dsub * 32 + i) * (L + 1) + ll];
+        const float zc = z0.x, zs = z0.y;
         ZrA = make_float2(zc, zc * A.z - zs * A.w);
         ZiA = make_float2(zs, zc * A.w + zs * A.z);
       };
@@ -409,6 +421,19 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
                 st[5 * 32] = make_float4(-R2s, -R2s, Hc, Hc);
                 st[6 * 32] = make_float4(Hs, Hs, -Hs, -Hs);
                 st[7 * 32] = make_float4(fabsf(dtau), 0.f, 0.f, 0.f);
+                // e^{i omega_0 tau} of this step for every lane of direction dd:
+                // L independent reseeds per lane, off the step loop's critical path
+                {
+                  float2 *row = seeds + ((size_t)dd * 32 + lane) * (L + 1);
+                  const float2 *w0 = sm.w0rev[warp] + dd * L;
+#pragma unroll 4
+                  for (int m = 0; m < L; ++m) {
+                    const float2 w = w0[m];
+                    float zs, zc;
+                    phasor_rev(w.x, w.y, tau.hi, tau.lo, zs, zc);
+                    row[m] = make_float2(zc, zs);
+                  }
+                }
                 const float am = (uint32_t)lane < mcnt ? fabsf(dtau) : 0.f;
                 const float amax =
                     __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(am)));
@@ -428,7 +453,7 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
               const float4 *st = setup + (size_t)dsub * kNSetupF4 * 32;
               for (uint32_t i = 0; i < mcnt; ++i) {
                 float2 zr, zi;
-                step_seed(st + i, zr, zi);
+                step_seed(st + i, i, zr, zi);
                 step_fast(st + i, zr, zi);
               }
             } else {
@@ -443,7 +468,7 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
                   // every point of the warp included: the straight-line step
                   // (the same products as the masked path with a full mask)
                   float2 zr, zi;
-                  step_seed(st, zr, zi);
+                  step_seed(st, i, zr, zi);
                   step_fast(st, zr, zi);
                 } else if (!__all_sync(0xffffffffu, all_out || nv == 0)) {
                   // one masked path for every lane of the warp (excluded lanes
@@ -483,10 +508,8 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
                   }
                   // phasors as two packed chains (uniform axis) or one reseed per
                   // point (non-uniform axis); amplitudes zeroed where masked out
-                  float zs, zc;
-                  phasor_rev(d_w0.hi, d_w0.lo, A.x, A.y, zs, zc);
-                  float2 ZrA = make_float2(zc, zc * A.z - zs * A.w);
-                  float2 ZiA = make_float2(zs, zc * A.w + zs * A.z);
+                  float2 ZrA, ZiA;
+                  step_seed(st, i, ZrA, ZiA);
                   float2 ZrB, ZiB;
                   rot2p(ZrA, ZiA, make_float2(X.z, X.w), make_float2(Y.x, Y.y),
                         make_float2(Y.z, Y.w), ZrB, ZiB);
@@ -556,12 +579,16 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
 }
 
 size_t near_smem_bytes(int dpw) {
-  return sizeof(NearSmemFixed<kNW>) + (size_t)kNW * 32 * dpw * kNSetupF4 * sizeof(float4);
+  return sizeof(NearSmemFixed<kNW>) + (size_t)kNW * 32 * dpw * kNSetupF4 * sizeof(float4) +
+         (size_t)kNW * near_seed_f2(dpw) * sizeof(float2);
 }
 
 template <int K>
 int launch_near_main(const FarMixedParams &p, int grid, cudaStream_t s) {
   const size_t smem = near_smem_bytes((int)p.dpw);
+  if (smem > kMaxSmemPerCta)
+    return fail(SR_ERR_INVALID, "work shape needs %zu bytes of shared memory per CTA (at most %zu)",
+                smem, kMaxSmemPerCta);
   cudaError_t e = cudaFuncSetAttribute(near_mixed_kernel<K, kNW>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_fail(e, "near_mixed smem attribute");

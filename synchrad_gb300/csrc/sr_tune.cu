@@ -153,6 +153,11 @@ extern "C" int sr_config_set(const sr_tracks *t, const sr_grid *g, int comp, int
     return fail(SR_ERR_INVALID, "lanes per direction %d (8, 16 or 32)", L);
   if (far && (st < 32 || st > 512 || (st & 31) != 0))
     return fail(SR_ERR_INVALID, "steps per stage %d (multiples of 32 in [32, 512])", st);
+  if (far && far_mixed_smem_bytes(32 / L, st) > 232448)
+    return fail(SR_ERR_INVALID,
+                "work shape (%d lanes per direction, %d steps per stage) needs %zu bytes of "
+                "shared memory per CTA (at most 232448)",
+                L, st, far_mixed_smem_bytes(32 / L, st));
   if (c->track_subsets < 0 || c->track_subsets > 64)
     return fail(SR_ERR_INVALID, "track subsets %d (0: default, at most 64)", c->track_subsets);
   const uint32_t n_dirs = g->n_theta * g->n_phi;
