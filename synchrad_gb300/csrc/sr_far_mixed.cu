@@ -121,7 +121,9 @@ constexpr int kMaxDpw = 4;  // directions per warp (omega tiles narrower than 32
 template <int W>
 struct SmemFixed {
   uint64_t bar[2];
-  uint64_t pad_[2];
+  uint32_t next_item;   // broadcast of the work item taken from the queue
+  uint32_t pad32_;
+  uint64_t pad_[1];
   DirConst dc[W][kMaxDpw];
   float2 w0rev[W][32];  // each lane's first frequency in revolutions (double-float)
   // followed by float4 setup[W][dpw][6][32], the two stage buffers of
@@ -182,7 +184,16 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
   const float w0g = nO > 0 ? (float)p.omega[0] : 0.f;
   const float dwg = (float)dw_glob, inv_dwg = (dwg != 0.f) ? 1.0f / dwg : 0.f;
 
-  for (uint32_t item = blockIdx.x; item < p.n_items; item += gridDim.x) {
+  // Work items: each CTA starts on its own, then takes the next one from a
+  // counter in the workspace (zeroed at launch), so that items of unequal cost
+  // (subsets of ragged tracks) keep every SM busy to the end.
+  auto next_item = [&]() -> uint32_t {
+    __syncthreads();  // every thread has read the previous item number
+    if (threadIdx.x == 0) sm.next_item = gridDim.x + atomicAdd(p.queue, 1u);
+    __syncthreads();
+    return sm.next_item;
+  };
+  for (uint32_t item = blockIdx.x; item < p.n_items; item = next_item()) {
     const uint32_t sub = item / p.n_groups, grp = item % p.n_groups;
     const uint32_t wt = grp * W + warp;
     const bool active_w = wt < n_wt;
@@ -779,6 +790,7 @@ int launch_far_mixed(FarMixedParams p, const FarMixedConfig &cfg, void *ws, size
   unsigned char *w = (unsigned char *)ws;
   size_t off = 256;
   p.status = (int *)w;
+  p.queue = (unsigned int *)(w + 128);  // in the zeroed 256-byte status block
   p.records = (float4 *)(w + off);
   off += ((size_t)p.total_steps * kRecBytes + 255) / 256 * 256;
   p.partial = (double *)(w + off);

@@ -69,6 +69,7 @@ struct FarMixedParams {
                        // [n_tracks][P][4] (A_theta, A_phi), near [n_tracks][P][8]
                        // (A_x, A_y, A_z complex, two floats of padding)
   int *status;
+  unsigned int *queue;   // work items handed out after each CTA's first (zeroed per launch)
   // outputs
   double *out[6];
 };
