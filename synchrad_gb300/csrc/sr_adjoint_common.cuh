@@ -58,14 +58,71 @@ __global__ void adj_globals_kernel(FarMixedParams p, float4 *wtab, AdjGlobals *g
   }
 }
 
-// Work items: ceil(n_body / steps_per_item) per track, as an exclusive prefix
-// (one block of 1024 threads, each scanning a contiguous run of tracks).
+// Snapshot segments of a track.  The forward writes snapshot k after step
+// f_k (the reference's state machine, SnapState); the snapshots that fire form
+// a run k_first .. k_last with increasing f_k, a step s enters every fired
+// snapshot with f_k >= s, and steps after the last fired one enter none.  So
+// the body steps fall into segments, segment i holding the steps after
+// f_{k_first + i - 1} up to f_{k_first + i}, each entering snapshots
+// k_first + i .. k_last.  Work items never cross a segment; a segment of n
+// steps makes ceil(n / per_item) items.
+struct SnapSegment {
+  uint32_t r0, r1;  // steps [r0, r1) of the item
+  uint32_t k0, k1;  // snapshots k0 .. k1 (inclusive) receive them
+};
+
+__device__ __forceinline__ uint32_t last_fired(const FarMixedParams &p, uint32_t t) {
+  SnapState st;
+  const uint32_t *snaps = p.snap_its + (size_t)t * p.snap_stride;
+  st.init(p.it_start[t], p.it_end[t], snaps, p.n_snaps);
+  uint32_t last = 0xffffffffu;
+  while (st.fire_it != SnapState::NEVER) {
+    last = st.k;
+    st.advance(p.it_start[t], p.it_end[t], snaps, p.n_snaps);
+  }
+  return last;
+}
+
+// Items of track t (count == nullptr) or the j-th of them (into *seg).
+__device__ __forceinline__ uint32_t track_segments(const FarMixedParams &p, uint32_t t,
+                                                   uint32_t per_item, uint32_t j,
+                                                   SnapSegment *seg) {
+  const uint32_t n_body = track_body(p, t);
+  if (n_body == 0) return 0;
+  const uint32_t k_last = last_fired(p, t);
+  if (k_last == 0xffffffffu) return 0;  // no snapshot fires: nothing to differentiate
+  SnapState st;
+  const uint32_t *snaps = p.snap_its + (size_t)t * p.snap_stride;
+  st.init(p.it_start[t], p.it_end[t], snaps, p.n_snaps);
+  uint32_t lo = 0, items = 0;
+  while (st.fire_it != SnapState::NEVER && lo < n_body) {
+    const uint32_t hi = (uint32_t)min<int64_t>(st.fire_it, (int64_t)n_body - 1);  // inclusive
+    if (hi >= lo) {
+      const uint32_t n = (hi - lo + per_item) / per_item;
+      if (seg != nullptr && j < items + n) {
+        seg->r0 = lo + (j - items) * per_item;
+        seg->r1 = min(hi + 1, seg->r0 + per_item);
+        seg->k0 = st.k;
+        seg->k1 = k_last;
+        return items + n;
+      }
+      items += n;
+      lo = hi + 1;
+    }
+    st.advance(p.it_start[t], p.it_end[t], snaps, p.n_snaps);
+  }
+  return items;
+}
+
+// Work items per track (snapshot segments cut into runs of steps_per_item),
+// as an exclusive prefix (one block of 1024 threads, each scanning a
+// contiguous run of tracks).
 __global__ void adj_items_kernel(FarMixedParams p, int64_t *item_off, uint32_t steps_per_item) {
   const uint32_t n = p.n_tracks;
   const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
   const uint32_t t0 = min(n, threadIdx.x * per), t1 = min(n, t0 + per);
   int64_t local = 0;
-  for (uint32_t t = t0; t < t1; ++t) local += (track_body(p, t) + steps_per_item - 1) / steps_per_item;
+  for (uint32_t t = t0; t < t1; ++t) local += track_segments(p, t, steps_per_item, 0, nullptr);
   __shared__ int64_t sums[1024];
   sums[threadIdx.x] = local;
   __syncthreads();
@@ -78,7 +135,7 @@ __global__ void adj_items_kernel(FarMixedParams p, int64_t *item_off, uint32_t s
   int64_t run = threadIdx.x ? sums[threadIdx.x - 1] : 0;
   for (uint32_t t = t0; t < t1; ++t) {
     item_off[t] = run;
-    run += (track_body(p, t) + steps_per_item - 1) / steps_per_item;
+    run += track_segments(p, t, steps_per_item, 0, nullptr);
   }
   if (threadIdx.x == blockDim.x - 1) item_off[n] = sums[blockDim.x - 1];
 }

@@ -297,8 +297,9 @@ __global__ void __launch_bounds__(kDW * 32, 1)
           const double Ar = val(acc.tr[q]), Ai = val(acc.ti[q]);
           const double Br = val(acc.pr[q]), Bi = val(acc.pi[q]);
           const uint64_t gti = (uint64_t)(j0 + m) + (uint64_t)nO * dir;
-          if (p.save_A != nullptr && ksnap == 0) {  // the adjoint's forward record
-            float4 *sa = reinterpret_cast<float4 *>(p.save_A) + (uint64_t)t * P + gti;
+          if (p.save_A != nullptr) {  // the adjoint's forward record, per snapshot
+            float4 *sa = reinterpret_cast<float4 *>(p.save_A) +
+                         ((uint64_t)t * p.n_snaps + ksnap) * P + gti;
             *sa = make_float4((float)Ar, (float)Ai, (float)Br, (float)Bi);
           }
           auto add = [&](int c, double v) {

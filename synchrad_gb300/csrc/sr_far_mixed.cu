@@ -318,8 +318,9 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
           const double Br = (double)o[2 * 32] + (double)o[6 * 32];
           const double Bi = (double)o[3 * 32] + (double)o[7 * 32];
           const uint64_t gti = (uint64_t)(j0 + m) + (uint64_t)nO * dir;
-          if (p.save_A != nullptr && ksnap == 0) {  // the adjoint's forward record
-            float4 *sa = reinterpret_cast<float4 *>(p.save_A) + (uint64_t)t * P + gti;
+          if (p.save_A != nullptr) {  // the adjoint's forward record, per snapshot
+            float4 *sa = reinterpret_cast<float4 *>(p.save_A) +
+                         ((uint64_t)t * p.n_snaps + ksnap) * P + gti;
             *sa = make_float4((float)Ar, (float)Ai, (float)Br, (float)Bi);
           }
           auto add = [&](int c, double v) {

@@ -65,9 +65,10 @@ struct FarMixedParams {
   float4 *records;     // [total_steps][4]
   double *partial;     // [n_sub][n_out][n_snaps][P]
   float *outer;        // [grid][W][K][8][32] compensated per-track sums
-  float *save_A;       // optional per-track amplitudes for the adjoints: far
-                       // [n_tracks][P][4] (A_theta, A_phi), near [n_tracks][P][8]
-                       // (A_x, A_y, A_z complex, two floats of padding)
+  float *save_A;       // optional per-track amplitudes for the adjoints, as each
+                       // snapshot writes them: far [n_tracks][n_snaps][P][4]
+                       // (A_theta, A_phi), near [n_tracks][n_snaps][P][8] (A_x, A_y,
+                       // A_z complex, two floats of padding)
   int *status;
   unsigned int *queue;   // work items handed out after each CTA's first (zeroed per launch)
   // outputs

@@ -286,8 +286,9 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
             Ai[c] = val(9 + c) + w * val(c);
           }
           const uint64_t gti = (uint64_t)(j0 + m) + (uint64_t)nO * dir;
-          if (p.save_A != nullptr && ksnap == 0) {  // the adjoint's forward record
-            float4 *sa = reinterpret_cast<float4 *>(p.save_A) + 2 * ((uint64_t)t * P + gti);
+          if (p.save_A != nullptr) {  // the adjoint's forward record, per snapshot
+            float4 *sa = reinterpret_cast<float4 *>(p.save_A) +
+                         2 * (((uint64_t)t * p.n_snaps + ksnap) * P + gti);
             sa[0] = make_float4((float)Ar[0], (float)Ai[0], (float)Ar[1], (float)Ai[1]);
             sa[1] = make_float4((float)Ar[2], (float)Ai[2], 0.f, 0.f);
           }

@@ -109,7 +109,7 @@ def test_far_stage_sizes_agree(stage):
     batch, grid, n = _setup(w)
     ref = _spectrum(batch, grid, n, _lib.SR_PREC_DOUBLE)
     _lib.lib().sr_config_clear()
-    bt.set_config(batch, grid, points_per_lane=16, lanes_per_direction=8, steps_per_stage=stage)
+    bt.set_config(batch, grid, points_per_lane=16, lanes_per_direction=16, steps_per_stage=stage)
     used = bt.current_config(batch, grid)
     assert used["steps_per_stage"] == stage and used["points_per_lane"] == 16
     got = _spectrum(batch, grid, n, _lib.SR_PREC_MIXED)
