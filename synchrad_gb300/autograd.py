@@ -32,12 +32,13 @@ class SpectrumLayout:
     offsets: torch.Tensor        # int64 [n+1] on the device
     it_start: torch.Tensor       # int32 [n]
     it_end: torch.Tensor         # int32 [n]
-    snap_its: torch.Tensor       # int32 [n] (one snapshot per track)
+    snap_its: torch.Tensor       # int32 [n][n_snaps] (each track's own snapshot row)
     dt: float
     grid: GridDevice
     workspace: Workspace
     mode: str = "far"
     precision: str = "mixed"     # forward arithmetic: 'mixed' or 'double-float' (far field)
+    n_snaps: int = 1             # snapshots per track (rows of snap_its)
 
     @property
     def n_tracks(self) -> int:
@@ -52,9 +53,13 @@ FarLayout = SpectrumLayout
 
 
 def make_layout(lengths, dt, host_axes, n, device="cuda", mode="far",
-                L_screen=0.0, precision="mixed", form_factor=None) -> SpectrumLayout:
+                L_screen=0.0, precision="mixed", form_factor=None,
+                n_snaps=1) -> SpectrumLayout:
     """Layout for tracks of the given lengths with the reference's per-track
-    rules (it_start = 0, itEnd = length, one snapshot at the last step).
+    rules (it_start = 0, itEnd = length, snapshot iterations
+    ``linspace(0, length, n_snaps + 1)[1:]``, synchrad/calc.py:297-301, 626-630);
+    with several snapshots the spectra are ``[n_snaps, ...]`` and each
+    snapshot's gradient flows to the steps it accumulated.
     host_axes: far (omega2pi, sinT, cosT, sinP, cosP), near (omega2pi, R,
     sinP, cosP) as from ``synchrad/calc.py:486-512``.
 
@@ -74,7 +79,9 @@ def make_layout(lengths, dt, host_axes, n, device="cuda", mode="far",
         raise ValueError("every track needs at least one step")
     offsets = np.zeros(lengths.size + 1, dtype=np.int64)
     np.cumsum(lengths, out=offsets[1:])
-    snaps = np.concatenate([snap_iterations((0, int(L)), 1) for L in lengths])
+    if int(n_snaps) < 1:
+        raise ValueError("at least one snapshot")
+    snaps = np.concatenate([snap_iterations((0, int(L)), int(n_snaps)) for L in lengths])
     t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)
     grid = make_grid(mode, host_axes, n, torch.float64, device, L_screen=L_screen,
                      form_factor=None if form_factor is None
@@ -82,13 +89,18 @@ def make_layout(lengths, dt, host_axes, n, device="cuda", mode="far",
     return SpectrumLayout(t(offsets), t(np.zeros(lengths.size, np.int32)),
                           t(lengths.astype(np.uint32).view(np.int32)),
                           t(snaps.astype(np.uint32).view(np.int32)), float(dt), grid,
-                          Workspace(device), mode, precision)
+                          Workspace(device), mode, precision, int(n_snaps))
 
 
 def _tracks_struct(coords, w, layout: FarLayout) -> TrackBatch:
     return TrackBatch(layout.n_tracks, torch.float64, int(coords[0].numel()), layout.offsets,
-                      list(coords), w, layout.it_start, layout.it_end, layout.snap_its, 1, 1,
-                      layout.dt)
+                      list(coords), w, layout.it_start, layout.it_end, layout.snap_its,
+                      layout.n_snaps, layout.n_snaps, layout.dt)
+
+
+def _spectrum_shape(layout: SpectrumLayout) -> tuple:
+    nO, nT, nP = layout.grid.n
+    return (nP, nT, nO) if layout.n_snaps == 1 else (layout.n_snaps, nP, nT, nO)
 
 
 _SAVED_FLOATS = {"far": 4, "near": 8}  # per point and track
@@ -105,11 +117,10 @@ class TotalSpectrum(torch.autograd.Function):
         wd = w.detach().contiguous().to(torch.float64)
         batch = _tracks_struct(coords, wd, layout)
         ts, gs = batch.c_struct(), layout.grid.c_struct()
-        nO, nT, nP = layout.grid.n
         P = layout.n_points
-        spec = torch.zeros((nP, nT, nO), dtype=torch.float64, device=x.device)
-        saved = torch.empty(layout.n_tracks * P * _SAVED_FLOATS[layout.mode], dtype=torch.float32,
-                            device=x.device)
+        spec = torch.zeros(_spectrum_shape(layout), dtype=torch.float64, device=x.device)
+        saved = torch.empty(layout.n_tracks * layout.n_snaps * P * _SAVED_FLOATS[layout.mode],
+                            dtype=torch.float32, device=x.device)
         df_fwd = layout.precision == "double-float"
         prec = _lib.SR_PREC_DF if df_fwd else _lib.SR_PREC_MIXED
         need = L.sr_workspace_bytes(ctypes.byref(ts), ctypes.byref(gs), 0, prec)
@@ -167,12 +178,11 @@ class SpectrumComps(torch.autograd.Function):
         wd = w.detach().contiguous().to(torch.float64)
         batch = _tracks_struct(coords, wd, layout)
         ts, gs = batch.c_struct(), layout.grid.c_struct()
-        nO, nT, nP = layout.grid.n
         P = layout.n_points
-        outs = [torch.zeros((nP, nT, nO), dtype=torch.float64, device=x.device)
+        outs = [torch.zeros(_spectrum_shape(layout), dtype=torch.float64, device=x.device)
                 for _ in range(_lib.N_OUT[cid])]
-        saved = torch.empty(layout.n_tracks * P * _SAVED_FLOATS[layout.mode], dtype=torch.float32,
-                            device=x.device)
+        saved = torch.empty(layout.n_tracks * layout.n_snaps * P * _SAVED_FLOATS[layout.mode],
+                            dtype=torch.float32, device=x.device)
         prec = _lib.SR_PREC_DF if layout.precision == "double-float" else _lib.SR_PREC_MIXED
         need = L.sr_workspace_bytes(ctypes.byref(ts), ctypes.byref(gs), cid, prec)
         if need < 0:
@@ -202,10 +212,9 @@ class SpectrumComps(torch.autograd.Function):
         cid = _lib.COMP_IDS[ctx.comp]
         batch = _tracks_struct(coords, wd, layout)
         ts, gs = batch.c_struct(), layout.grid.c_struct()
-        nO, nT, nP = layout.grid.n
         dev = coords[0].device
         g = [(gr.detach().contiguous().to(torch.float64) if gr is not None
-              else torch.zeros((nP, nT, nO), dtype=torch.float64, device=dev))
+              else torch.zeros(_spectrum_shape(layout), dtype=torch.float64, device=dev))
              for gr in grad_outs]
         grads = [torch.empty_like(c) for c in coords]
         gw = torch.empty(layout.n_tracks, dtype=torch.float64, device=dev)

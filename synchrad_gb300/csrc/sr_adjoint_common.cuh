@@ -96,7 +96,8 @@ __device__ __forceinline__ uint32_t track_segments(const FarMixedParams &p, uint
   st.init(p.it_start[t], p.it_end[t], snaps, p.n_snaps);
   uint32_t lo = 0, items = 0;
   while (st.fire_it != SnapState::NEVER && lo < n_body) {
-    const uint32_t hi = (uint32_t)min<int64_t>(st.fire_it, (int64_t)n_body - 1);  // inclusive
+    const int64_t last_body = (int64_t)n_body - 1;
+    const uint32_t hi = (uint32_t)(st.fire_it < last_body ? st.fire_it : last_body);  // inclusive
     if (hi >= lo) {
       const uint32_t n = (hi - lo + per_item) / per_item;
       if (seg != nullptr && j < items + n) {

@@ -65,9 +65,11 @@ struct AdjParams {
 // at point gi: M = (xx, xy, yy) of the quadratic comps (2 dt^2 included) or V
 // = (th re, th im, ph re, ph im) of the linear ones (dt and FormFactor
 // included), in FP64.
-__device__ __forceinline__ void point_sens(const AdjParams &a, uint64_t gi, double out[4]) {
+__device__ __forceinline__ void point_sens(const AdjParams &a, uint32_t ksnap, uint64_t gi,
+                                           double out[4]) {
   const FarMixedParams &p = a.f;
   const uint32_t nO = p.n_omega, nT = p.n_theta;
+  const uint64_t gk = (uint64_t)ksnap * nO * nT * p.n_phi + gi;  // snapshot ksnap's slot
   const uint64_t d = gi / nO;
   const uint32_t m = (uint32_t)(gi - d * nO);
   const uint32_t iT = (uint32_t)(d % nT), iP = (uint32_t)(d / nT);
@@ -76,7 +78,7 @@ __device__ __forceinline__ void point_sens(const AdjParams &a, uint64_t gi, doub
   // output unit vectors x, y, z on (theta-hat, phi-hat)
   const double bt[3] = {cT * cP, cT * sP, -sT}, bp[3] = {-sP, cP, 0.0};
   const double s2 = 2.0 * p.dt * p.dt;
-  auto g = [&](int k) { return a.grad_out[k][gi]; };
+  auto g = [&](int k) { return a.grad_out[k][gk]; };
   out[0] = out[1] = out[2] = out[3] = 0.0;
   switch (p.comp) {
     case SR_COMP_TOTAL:
@@ -123,9 +125,10 @@ __global__ void adj_prep_kernel(AdjParams a) {
   const uint64_t n_dirs = (uint64_t)nT * p.n_phi;
   const uint64_t P = n_dirs * p.n_omega;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P; i += stride) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P * p.n_snaps;
+       i += stride) {
     double v[4];
-    point_sens(a, i, v);
+    point_sens(a, (uint32_t)(i / P), i % P, v);
     a.gcst[i] = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
   }
   for (uint64_t d = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; d < n_dirs; d += stride) {
@@ -153,15 +156,17 @@ __global__ void adj_weight_partial_far_kernel(AdjParams a, uint64_t P, uint32_t 
   const uint64_t g0 = (uint64_t)b * chunk, g1 = min(P, g0 + chunk);
   double acc = 0.0;
   for (uint64_t g = g0 + threadIdx.x; g < g1; g += blockDim.x) {
-    double v[4];
-    point_sens(a, g, v);
-    const float4 A = a.save_A[(uint64_t)t * P + g];
-    const double ar = A.x, ai = A.y, br = A.z, bi = A.w;
-    if (a.linear)  // Re(conj(V) . A)
-      acc += v[0] * ar + v[1] * ai + v[2] * br + v[3] * bi;
-    else           // A^H M A
-      acc += v[0] * (ar * ar + ai * ai) + 2.0 * v[1] * (ar * br + ai * bi) +
-             v[2] * (br * br + bi * bi);
+    for (uint32_t k = 0; k < a.f.n_snaps; ++k) {  // a snapshot that never fired has A = 0
+      double v[4];
+      point_sens(a, k, g, v);
+      const float4 A = a.save_A[((uint64_t)t * a.f.n_snaps + k) * P + g];
+      const double ar = A.x, ai = A.y, br = A.z, bi = A.w;
+      if (a.linear)  // Re(conj(V) . A)
+        acc += v[0] * ar + v[1] * ai + v[2] * br + v[3] * bi;
+      else           // A^H M A
+        acc += v[0] * (ar * ar + ai * ai) + 2.0 * v[1] * (ar * br + ai * bi) +
+               v[2] * (br * br + bi * bi);
+    }
   }
   __shared__ double red[kWeightThreads];
   red[threadIdx.x] = acc;
@@ -299,8 +304,9 @@ __global__ void __launch_bounds__(W * 32, 2) adj_far_kernel(AdjParams a) {
     const uint32_t t = lo;
     const int64_t base = p.offsets[t];
     const uint32_t n_body = track_body(p, t);
-    const uint32_t r0 = (uint32_t)(item - a.item_off[t]) * kASteps;
-    const uint32_t r1 = min(n_body, r0 + kASteps);
+    SnapSegment seg{0, 0, 0, 0};
+    track_segments(p, t, (uint32_t)kASteps, (uint32_t)(item - a.item_off[t]), &seg);
+    const uint32_t r0 = seg.r0, r1 = seg.r1;  // the steps enter snapshots seg.k0 .. seg.k1
     const uint32_t has_prev = r0 > 0 ? 1u : 0u;
     const uint32_t n_rec = r1 - r0 + has_prev;
     if (threadIdx.x == 0) {  // the item's records in one bulk copy
@@ -351,14 +357,21 @@ __global__ void __launch_bounds__(W * 32, 2) adj_far_kernel(AdjParams a) {
         for (int e = 0; e < 2; ++e) {
           if (m + e < nO) {
             const uint64_t gi = dj * nO + m + e;
-            const float4 C = a.gcst[gi];
             wv[e] = a.wtab[m + e];
-            if (a.linear) {
-              u[e] = make_float4(swt * C.x, swt * C.y, swt * C.z, swt * C.w);
-            } else {
-              const float4 A = a.save_A[(uint64_t)t * P + gi];
-              u[e] = make_float4(wt * (C.x * A.x + C.y * A.z), wt * (C.x * A.y + C.y * A.w),
-                                 wt * (C.y * A.x + C.z * A.z), wt * (C.y * A.y + C.z * A.w));
+            // U summed over the snapshots these steps enter
+            u[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (uint32_t k = seg.k0; k <= seg.k1; ++k) {
+              const float4 C = a.gcst[(uint64_t)k * P + gi];
+              if (a.linear) {
+                u[e].x += swt * C.x; u[e].y += swt * C.y;
+                u[e].z += swt * C.z; u[e].w += swt * C.w;
+              } else {
+                const float4 A = a.save_A[((uint64_t)t * p.n_snaps + k) * P + gi];
+                u[e].x += wt * (C.x * A.x + C.y * A.z);
+                u[e].y += wt * (C.x * A.y + C.y * A.w);
+                u[e].z += wt * (C.y * A.x + C.z * A.z);
+                u[e].w += wt * (C.y * A.y + C.z * A.w);
+              }
             }
             w[e] = make_float4(wv[e].z * u[e].x, -wv[e].z * u[e].y, wv[e].z * u[e].z,
                                -wv[e].z * u[e].w);
@@ -530,13 +543,13 @@ struct AdjLayout {
 };
 
 AdjLayout adj_layout(int64_t total_steps, uint64_t P, uint32_t n_omega, uint64_t n_dirs,
-                     uint32_t n_tracks) {
+                     uint32_t n_tracks, uint32_t n_snaps) {
   auto up = [](size_t v) { return (v + 255) / 256 * 256; };
   AdjLayout l;
   l.w_chunks = adj_weight_chunks(P, n_tracks, device_sm_count());
   l.records = 256;
   l.gcst = l.records + up((size_t)total_steps * kRecBytes);
-  l.wtab = l.gcst + up((size_t)P * 16);
+  l.wtab = l.gcst + up((size_t)P * 16 * (n_snaps ? n_snaps : 1));
   l.dirtab = l.wtab + up((size_t)n_omega * 16);
   l.glob = l.dirtab + up((size_t)n_dirs * 64);
   l.item_off = l.glob + 256;
@@ -551,8 +564,8 @@ int check_adjoint_args(const sr_tracks *t, const sr_grid *g, void *const *out,
   int rc = validate_spectrum_args(t, g, comp, SR_PREC_MIXED, out);
   if (rc) return rc;
   if (g->mode != SR_MODE_FAR) return fail(SR_ERR_UNSUPPORTED, "the adjoint is far field only");
-  if (t->n_snaps != 1)
-    return fail(SR_ERR_UNSUPPORTED, "the adjoint differentiates a single snapshot (n_snaps = 1)");
+  if (t->n_snaps < 1)
+    return fail(SR_ERR_UNSUPPORTED, "the adjoint needs at least one snapshot (n_snaps >= 1)");
   return SR_OK;
 }
 
@@ -573,7 +586,7 @@ extern "C" int sr_far_forward_saved(const sr_tracks *t, const sr_grid *g, int co
   const uint64_t P = (uint64_t)g->n_omega * g->n_theta * g->n_phi;
   if (P == 0 || t->n_tracks == 0) return SR_OK;
   cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = cudaMemsetAsync(saved_A, 0, (size_t)t->n_tracks * P * 16, s);
+  cudaError_t e = cudaMemsetAsync(saved_A, 0, (size_t)t->n_tracks * t->n_snaps * P * 16, s);
   if (e != cudaSuccess) return cuda_fail(e, "saved_A reset");
   FarMixedParams p = make_far_mixed_params(t, g, comp, out);
   p.save_A = saved_A;
@@ -605,7 +618,7 @@ extern "C" int64_t sr_far_backward_workspace_bytes(const sr_tracks *t, const sr_
   if (!t || !g) return -1;
   const uint64_t n_dirs = (uint64_t)g->n_theta * g->n_phi;
   return (int64_t)adj_layout(t->total_steps, n_dirs * g->n_omega, g->n_omega, n_dirs,
-                             t->n_tracks)
+                             t->n_tracks, t->n_snaps)
       .total;
 }
 
@@ -647,7 +660,7 @@ extern "C" int sr_far_backward(const sr_tracks *t, const sr_grid *g, int comp,
     e = cudaMemsetAsync(grad_weight, 0, (size_t)t->n_tracks * 8, s);
     return e == cudaSuccess ? SR_OK : cuda_fail(e, "gradient reset");
   }
-  const AdjLayout lay = adj_layout(t->total_steps, P, g->n_omega, n_dirs, t->n_tracks);
+  const AdjLayout lay = adj_layout(t->total_steps, P, g->n_omega, n_dirs, t->n_tracks, t->n_snaps);
   if (!workspace || workspace_bytes < lay.total)
     return fail(SR_ERR_WORKSPACE, "workspace of %zu bytes needed, %zu given", lay.total,
                 workspace_bytes);
@@ -674,6 +687,9 @@ extern "C" int sr_far_backward(const sr_tracks *t, const sr_grid *g, int comp,
 
   e = cudaMemsetAsync(w, 0, 256, s);
   if (e != cudaSuccess) return cuda_fail(e, "status reset");
+  // steps that enter no snapshot (after the last one written) are not visited
+  e = cudaMemsetAsync(a.gstep, 0, (size_t)t->total_steps * kAG * 8, s);
+  if (e != cudaSuccess) return cuda_fail(e, "gradient reset");
   const int n_sm = device_sm_count();
   const int64_t step_blocks = std::max<int64_t>(
       1, std::min<int64_t>((t->total_steps + 255) / 256, (int64_t)n_sm * 128));

@@ -66,21 +66,22 @@ struct NearAdjParams {
 // Point sensitivity (FP64) of the loss to (A_x, A_y, A_z) at point gi for the
 // output gradients g_k: quadratic comps 2 dt^2 (g_x, g_y, g_z) in v[0..2];
 // cartesian_complex V_k = dt (g_k,re + i g_k,im) e^{-i omega L} in v[0..5].
-__device__ __forceinline__ void near_point_sens(const NearAdjParams &a, uint64_t gi,
-                                                double v[6]) {
+__device__ __forceinline__ void near_point_sens(const NearAdjParams &a, uint32_t ksnap,
+                                                uint64_t gi, double v[6]) {
   const FarMixedParams &p = a.f;
   const double s2 = 2.0 * p.dt * p.dt;
+  const uint64_t gk = (uint64_t)ksnap * p.n_omega * p.n_theta * p.n_phi + gi;  // snapshot slot
   for (int k = 0; k < 6; ++k) v[k] = 0.0;
   if (p.comp == SR_COMP_TOTAL) {
-    v[0] = v[1] = v[2] = s2 * a.grad_out[0][gi];
+    v[0] = v[1] = v[2] = s2 * a.grad_out[0][gk];
   } else if (p.comp == SR_COMP_CARTESIAN) {
-    for (int k = 0; k < 3; ++k) v[k] = s2 * a.grad_out[k][gi];
+    for (int k = 0; k < 3; ++k) v[k] = s2 * a.grad_out[k][gk];
   } else {  // cartesian_complex (FormFactor not applied, as the reference)
     const double w = p.omega[gi % p.n_omega];
     double sL, cL;
     sincos(w * p.L_screen, &sL, &cL);
     for (int k = 0; k < 3; ++k) {
-      const double gr = a.grad_out[2 * k][gi], gim = a.grad_out[2 * k + 1][gi];
+      const double gr = a.grad_out[2 * k][gk], gim = a.grad_out[2 * k + 1][gk];
       v[2 * k] = p.dt * (gr * cL + gim * sL);
       v[2 * k + 1] = p.dt * (gim * cL - gr * sL);
     }
@@ -96,14 +97,16 @@ __global__ void nadj_weight_partial_kernel(NearAdjParams a, uint64_t P, uint32_t
   const uint64_t g0 = (uint64_t)b * chunk, g1 = min(P, g0 + chunk);
   double acc = 0.0;
   for (uint64_t g = g0 + threadIdx.x; g < g1; g += blockDim.x) {
-    double v[6];
-    near_point_sens(a, g, v);
-    const float4 A0 = a.save_A[2 * ((uint64_t)t * P + g)];
-    const float4 A1 = a.save_A[2 * ((uint64_t)t * P + g) + 1];
-    const double re[3] = {A0.x, A0.z, A1.x}, im[3] = {A0.y, A0.w, A1.y};
-    for (int k = 0; k < 3; ++k)
-      acc += a.linear ? v[2 * k] * re[k] + v[2 * k + 1] * im[k]
-                      : v[k] * (re[k] * re[k] + im[k] * im[k]);
+    for (uint32_t ks = 0; ks < a.f.n_snaps; ++ks) {  // a snapshot that never fired has A = 0
+      double v[6];
+      near_point_sens(a, ks, g, v);
+      const uint64_t ia = 2 * (((uint64_t)t * a.f.n_snaps + ks) * P + g);
+      const float4 A0 = a.save_A[ia], A1 = a.save_A[ia + 1];
+      const double re[3] = {A0.x, A0.z, A1.x}, im[3] = {A0.y, A0.w, A1.y};
+      for (int k = 0; k < 3; ++k)
+        acc += a.linear ? v[2 * k] * re[k] + v[2 * k + 1] * im[k]
+                        : v[k] * (re[k] * re[k] + im[k] * im[k]);
+    }
   }
   __shared__ double red[kWeightThreads];
   red[threadIdx.x] = acc;
@@ -132,9 +135,10 @@ __global__ void nadj_prep_kernel(NearAdjParams a) {
   const uint64_t n_scr = (uint64_t)nR * p.n_phi;
   const uint64_t P = n_scr * p.n_omega;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P; i += stride) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P * p.n_snaps;
+       i += stride) {
     double v[6];
-    near_point_sens(a, i, v);
+    near_point_sens(a, (uint32_t)(i / P), i % P, v);
     a.gcst[2 * i] = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
     a.gcst[2 * i + 1] = make_float4((float)v[4], (float)v[5], 0.f, 0.f);
   }
@@ -272,8 +276,9 @@ __global__ void __launch_bounds__(W * 32, 2) nadj_kernel(NearAdjParams a) {
     const uint32_t t = lo;
     const int64_t base = p.offsets[t];
     const uint32_t n_body = track_body(p, t);
-    const uint32_t r0 = (uint32_t)(item - a.item_off[t]) * kNASteps;
-    const uint32_t r1 = min(n_body, r0 + kNASteps);
+    SnapSegment seg{0, 0, 0, 0};
+    track_segments(p, t, (uint32_t)kNASteps, (uint32_t)(item - a.item_off[t]), &seg);
+    const uint32_t r0 = seg.r0, r1 = seg.r1;  // the steps enter snapshots seg.k0 .. seg.k1
     const uint32_t has_prev = r0 > 0 ? 1u : 0u;
     const uint32_t n_rec = r1 - r0 + has_prev;
     if (threadIdx.x == 0) {  // the item's records in one bulk copy
@@ -327,17 +332,23 @@ __global__ void __launch_bounds__(W * 32, 2) nadj_kernel(NearAdjParams a) {
         for (int e = 0; e < 2; ++e) {
           if (m + e < nO) {
             const uint64_t gi = dj * nO + m + e;
-            const float4 A0 = a.save_A[2 * ((uint64_t)t * P + gi)];
-            const float4 A1 = a.save_A[2 * ((uint64_t)t * P + gi) + 1];
-            const float4 C0 = a.gcst[2 * gi], C1 = a.gcst[2 * gi + 1];
-            if (a.linear) {  // U_k = sqrt(w) V_k
-              ar[e][0] = swt * C0.x; ai[e][0] = swt * C0.y;
-              ar[e][1] = swt * C0.z; ai[e][1] = swt * C0.w;
-              ar[e][2] = swt * C1.x; ai[e][2] = swt * C1.y;
-            } else {         // U_k = w g'_k A_k
-              ar[e][0] = wt * C0.x * A0.x; ai[e][0] = wt * C0.x * A0.y;
-              ar[e][1] = wt * C0.y * A0.z; ai[e][1] = wt * C0.y * A0.w;
-              ar[e][2] = wt * C0.z * A1.x; ai[e][2] = wt * C0.z * A1.y;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) ar[e][k] = ai[e][k] = 0.f;
+            // U summed over the snapshots these steps enter
+            for (uint32_t ks = seg.k0; ks <= seg.k1; ++ks) {
+              const uint64_t ic = 2 * ((uint64_t)ks * P + gi);
+              const float4 C0 = a.gcst[ic], C1 = a.gcst[ic + 1];
+              if (a.linear) {  // U_k = sqrt(w) V_k
+                ar[e][0] += swt * C0.x; ai[e][0] += swt * C0.y;
+                ar[e][1] += swt * C0.z; ai[e][1] += swt * C0.w;
+                ar[e][2] += swt * C1.x; ai[e][2] += swt * C1.y;
+              } else {         // U_k = w g'_k A_k
+                const uint64_t ia = 2 * (((uint64_t)t * p.n_snaps + ks) * P + gi);
+                const float4 A0 = a.save_A[ia], A1 = a.save_A[ia + 1];
+                ar[e][0] += wt * C0.x * A0.x; ai[e][0] += wt * C0.x * A0.y;
+                ar[e][1] += wt * C0.y * A0.z; ai[e][1] += wt * C0.y * A0.w;
+                ar[e][2] += wt * C0.z * A1.x; ai[e][2] += wt * C0.z * A1.y;
+              }
             }
             wv[e] = a.wtab[m + e];
           } else {
@@ -509,13 +520,13 @@ struct NearAdjLayout {
 };
 
 NearAdjLayout nadj_layout(int64_t total_steps, uint64_t P, uint32_t n_omega, uint64_t n_scr,
-                          uint32_t n_tracks) {
+                          uint32_t n_tracks, uint32_t n_snaps) {
   auto up = [](size_t v) { return (v + 255) / 256 * 256; };
   NearAdjLayout l;
   l.w_chunks = adj_weight_chunks(P, n_tracks, device_sm_count());
   l.records = 256;
   l.gcst = l.records + up((size_t)total_steps * kRecBytes);
-  l.wtab = l.gcst + up((size_t)P * 32);
+  l.wtab = l.gcst + up((size_t)P * 32 * (n_snaps ? n_snaps : 1));
   l.sctab = l.wtab + up((size_t)n_omega * 16);
   l.glob = l.sctab + up((size_t)n_scr * 16);
   l.item_off = l.glob + 256;
@@ -530,8 +541,8 @@ int check_near_adjoint_args(const sr_tracks *t, const sr_grid *g, void *const *o
   int rc = validate_spectrum_args(t, g, comp, SR_PREC_MIXED, out);
   if (rc) return rc;
   if (g->mode != SR_MODE_NEAR) return fail(SR_ERR_UNSUPPORTED, "near-field adjoint: mode near");
-  if (t->n_snaps != 1)
-    return fail(SR_ERR_UNSUPPORTED, "the adjoint differentiates a single snapshot (n_snaps = 1)");
+  if (t->n_snaps < 1)
+    return fail(SR_ERR_UNSUPPORTED, "the adjoint needs at least one snapshot (n_snaps >= 1)");
   return SR_OK;
 }
 
@@ -550,7 +561,7 @@ extern "C" int sr_near_forward_saved(const sr_tracks *t, const sr_grid *g, int c
   const uint64_t P = (uint64_t)g->n_omega * g->n_theta * g->n_phi;
   if (P == 0 || t->n_tracks == 0) return SR_OK;
   cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = cudaMemsetAsync(saved_A, 0, (size_t)t->n_tracks * P * 32, s);
+  cudaError_t e = cudaMemsetAsync(saved_A, 0, (size_t)t->n_tracks * t->n_snaps * P * 32, s);
   if (e != cudaSuccess) return cuda_fail(e, "saved_A reset");
   FarMixedParams p = make_far_mixed_params(t, g, comp, out);
   p.save_A = saved_A;
@@ -573,7 +584,7 @@ extern "C" int64_t sr_near_backward_workspace_bytes(const sr_tracks *t, const sr
   if (!t || !g) return -1;
   const uint64_t n_scr = (uint64_t)g->n_theta * g->n_phi;
   return (int64_t)nadj_layout(t->total_steps, n_scr * g->n_omega, g->n_omega, n_scr,
-                              t->n_tracks)
+                              t->n_tracks, t->n_snaps)
       .total;
 }
 
@@ -611,7 +622,8 @@ extern "C" int sr_near_backward(const sr_tracks *t, const sr_grid *g, int comp,
     e = cudaMemsetAsync(grad_weight, 0, (size_t)t->n_tracks * 8, s);
     return e == cudaSuccess ? SR_OK : cuda_fail(e, "gradient reset");
   }
-  const NearAdjLayout lay = nadj_layout(t->total_steps, P, g->n_omega, n_scr, t->n_tracks);
+  const NearAdjLayout lay =
+      nadj_layout(t->total_steps, P, g->n_omega, n_scr, t->n_tracks, t->n_snaps);
   if (!workspace || workspace_bytes < lay.total)
     return fail(SR_ERR_WORKSPACE, "workspace of %zu bytes needed, %zu given", lay.total,
                 workspace_bytes);
@@ -638,6 +650,9 @@ extern "C" int sr_near_backward(const sr_tracks *t, const sr_grid *g, int comp,
 
   e = cudaMemsetAsync(w, 0, 256, s);
   if (e != cudaSuccess) return cuda_fail(e, "status reset");
+  // steps that enter no snapshot (after the last one written) are not visited
+  e = cudaMemsetAsync(a.gstep, 0, (size_t)t->total_steps * kNAG * 8, s);
+  if (e != cudaSuccess) return cuda_fail(e, "gradient reset");
   const int n_sm = device_sm_count();
   const int64_t step_blocks = std::max<int64_t>(
       1, std::min<int64_t>((t->total_steps + 255) / 256, (int64_t)n_sm * 128));

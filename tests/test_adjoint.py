@@ -223,7 +223,7 @@ def test_adjoint_rejects_unsupported():
     from synchrad_gb300 import batch as bt
     tracks, dt, axes, n, _ = make_case(True)
     L = _lib.lib()
-    tb = bt.pack_tracks(tracks, np.float64, 2, dt, device="cuda")  # two snapshots
+    tb = bt.pack_tracks(tracks, np.float64, 0, dt, device="cuda")  # no snapshot
     grid = bt.make_grid("far", axes, n, torch.float64, "cuda")
     S = torch.zeros((n[2], n[1], n[0]), dtype=torch.float64, device="cuda")
     A = torch.zeros(len(tracks) * int(np.prod(n)) * 4, dtype=torch.float32, device="cuda")
