@@ -200,8 +200,8 @@ int sr_config_get(const sr_tracks *tracks, const sr_grid *grid, int comp, int pr
  * tuned in an earlier process): points_per_lane (far 8/16/24/32, near 8/16),
  * lanes_per_direction (8/16/32), steps_per_stage (far: multiple of 32 in
  * [32, 512]) and track_subsets (0: default, at most 64) are used, the rest is
- * derived.  Shapes whose shared memory exceeds a CTA's 227 KB (8 lanes per
- * direction with stages above 256 steps) are refused with SR_ERR_INVALID. */
+ * derived.  A shape whose shared memory would exceed a CTA's 227 KB is
+ * refused with SR_ERR_INVALID. */
 int sr_config_set(const sr_tracks *tracks, const sr_grid *grid, int comp, int precision,
                   const sr_config *config);
 

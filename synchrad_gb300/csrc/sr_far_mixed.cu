@@ -125,15 +125,9 @@ struct SmemFixed {
   uint32_t pad32_;
   uint64_t pad_[1];
   DirConst dc[W][kMaxDpw];
-  float2 w0rev[W][32];  // each lane's first frequency in revolutions (double-float)
-  // followed by float4 setup[W][dpw][6][32], the two stage buffers of
-  // p.stage_steps step records each, and
-  // float2 seeds[W][dpw][32 steps][L + 1]: e^{i omega_0 tau} of every lane and step
+  // followed by float4 setup[W][dpw][6][32], then the two stage buffers of
+  // p.stage_steps step records each
 };
-
-// float2 per warp in the seed table: dpw directions x 32 steps x (L + 1) (one
-// float2 of padding per row keeps the setup's stores free of bank conflicts)
-__host__ __device__ constexpr int far_seed_f2(int dpw) { return dpw * 32 * (32 / dpw + 1); }
 
 // Kernel of the mixed-precision far field.  K points per lane (two packed
 // rotation chains of K/2), L lanes per direction, 32/L directions per warp.
@@ -151,8 +145,6 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
   float4 *stage_buf[2];
   stage_buf[0] = setup_all + (size_t)W * 32 * dpw * 6;
   stage_buf[1] = stage_buf[0] + (size_t)S * kRecF4;
-  float2 *seeds = reinterpret_cast<float2 *>(stage_buf[1] + (size_t)S * kRecF4) +
-                  (size_t)warp * far_seed_f2(dpw);
   constexpr int KP = K / 2, HP = KP / 2;
 
   if (threadIdx.x == 0) {
@@ -226,10 +218,7 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
 
     // Lane omega constants (revolutions) and uniformity of its chunk.
     const double w0d = nv > 0 ? p.omega[j0] : 0.0;
-    {
-      const df d_w0 = df_from_double(w0d * inv2pi);
-      sm.w0rev[warp][lane] = make_float2(d_w0.hi, d_w0.lo);
-    }
+    const df d_w0 = df_from_double(w0d * inv2pi);
     const float w0f = (float)w0d, dwf = (float)dw_glob;
     const float inv_dwf = (dwf != 0.f) ? 1.0f / dwf : 0.f;
     bool uniform = true;
@@ -465,19 +454,6 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
                 }
                 st[5 * 32] = make_float4(fabsf(dtau), __int_as_float(jfc), __int_as_float(jlc),
                                          __uint_as_float((uint32_t)jfu | ((uint32_t)(jlu + 1) << 16)));
-                // e^{i omega_0 tau} of this step for every lane of direction dd:
-                // L independent reseeds per lane, off the step loop's critical path
-                {
-                  float2 *row = seeds + ((size_t)dd * 32 + lane) * (L + 1);
-                  const float2 *w0 = sm.w0rev[warp] + dd * L;
-#pragma unroll 4
-                  for (int m = 0; m < L; ++m) {
-                    const float2 w = w0[m];
-                    float zs, zc;
-                    phasor_rev(w.x, w.y, tau.hi, tau.lo, zs, zc);
-                    row[m] = make_float2(zc, zs);
-                  }
-                }
                 // largest |dtau| of the chunk: decides the chunk's fast loop
                 const float am = (uint32_t)lane < mcnt ? fabsf(dtau) : 0.f;
                 const float amax = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(am)));
@@ -493,13 +469,13 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
             // with a uniform axis and no snapshot write, runs the tight loop.
             const bool fire_here = snap.fire_it >= (int64_t)(s0 + c0) &&
                                    snap.fire_it < (int64_t)(s0 + c0 + mcnt);
-            // The first pair's phasors of step i of the chunk: the reseed
-            // e^{i omega_0 tau} (from the setup's seed table) and its product
-            // with R = e^{i d_omega tau}.
-            auto step_seed = [&](const float4 *st, uint32_t i, float2 &ZrA, float2 &ZiA) {
+            // The first pair's phasors of one step: the reseed e^{i omega_0 tau}
+            // (the lane's own sin/cos, interleaved with the other steps' sums)
+            // and its product with R = e^{i d_omega tau}.
+            auto step_seed = [&](const float4 *st, uint32_t, float2 &ZrA, float2 &ZiA) {
               const float4 A = st[0];
-              const float2 z0 = seeds[((size_t)dsub * 32 + i) * (L + 1) + ll];
-              const float zc = z0.x, zs = z0.y;
+              float zs, zc;
+              phasor_rev(d_w0.hi, d_w0.lo, A.x, A.y, zs, zc);
               ZrA = make_float2(zc, zc * A.z - zs * A.w);
               ZiA = make_float2(zs, zc * A.w + zs * A.z);
             };
@@ -690,8 +666,7 @@ constexpr int kW = 8;  // warps per CTA
 
 size_t smem_bytes(int dpw, int stage) {
   return sizeof(SmemFixed<kW>) + (size_t)kW * 32 * dpw * 6 * sizeof(float4) +
-         (size_t)2 * stage * kRecF4 * sizeof(float4) +
-         (size_t)kW * far_seed_f2(dpw) * sizeof(float2);
+         (size_t)2 * stage * kRecF4 * sizeof(float4);
 }
 
 template <int K>

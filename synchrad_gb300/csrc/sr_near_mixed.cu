@@ -95,14 +95,8 @@ struct NearSmemFixed {
   uint32_t pad32_;
   uint64_t pad_[1];
   ScreenConst sc[W][kNMaxDpw];
-  float2 w0rev[W][32];  // each lane's first frequency in revolutions (double-float)
-  // followed by float4 setup[W][dpw][kNSetupF4][32] and
-  // float2 seeds[W][dpw][32 steps][L + 1]: e^{i omega_0 tau} of every lane and step
+  // followed by float4 setup[W][dpw][kNSetupF4][32]
 };
-
-// float2 per warp in the seed table: dpw directions x 32 steps x (L + 1) (one
-// float2 of padding per row keeps the setup's stores free of bank conflicts)
-__host__ __device__ constexpr int near_seed_f2(int dpw) { return dpw * 32 * (32 / dpw + 1); }
 
 // Packed accumulators of one lane: six complex sums for K points.
 template <int K>
@@ -135,8 +129,6 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int dsub = lane / L, ll = lane % L;
   float4 *setup = setup_all + (size_t)warp * 32 * dpw * kNSetupF4;
-  float2 *seeds = reinterpret_cast<float2 *>(setup_all + (size_t)W * 32 * dpw * kNSetupF4) +
-                  (size_t)warp * near_seed_f2(dpw);
 
   if (threadIdx.x == 0) {
     mbar_init(&sm.bar[0], 1);
@@ -188,10 +180,7 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
       c.tprev_h = 0.f; c.tprev_l = 0.f;
     }
     const double w0d = nv > 0 ? p.omega[j0] : 0.0;
-    {
-      const df d_w0 = df_from_double(w0d * inv2pi);
-      sm.w0rev[warp][lane] = make_float2(d_w0.hi, d_w0.lo);
-    }
+    const df d_w0 = df_from_double(w0d * inv2pi);
     const float w0f = (float)w0d, dwf = (float)dw_glob;
     bool uniform = true;
     float wabs_min = 3.0e38f, wabs_max = 0.f;
@@ -313,13 +302,13 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
         }
       };
 
-      // The first pair's phasors of step i of the chunk: the reseed
-      // e^{i omega_0 tau} (from the setup's seed table) and its product with
-      // R = e^{i d_omega tau}.
-      auto step_seed = [&](const float4 *st, uint32_t i, float2 &ZrA, float2 &ZiA) {
+      // The first pair's phasors of one step: the reseed e^{i omega_0 tau}
+      // (the lane's own sin/cos, interleaved with the other steps' sums) and
+      // its product with R = e^{i d_omega tau}.
+      auto step_seed = [&](const float4 *st, uint32_t, float2 &ZrA, float2 &ZiA) {
         const float4 A = st[0];
-        const float2 z0 = seeds[((size_t)dsub * 32 + i) * (L + 1) + ll];
-        const float zc = z0.x, zs = z0.y;
+        float zs, zc;
+        phasor_rev(d_w0.hi, d_w0.lo, A.x, A.y, zs, zc);
         ZrA = make_float2(zc, zc * A.z - zs * A.w);
         ZiA = make_float2(zs, zc * A.w + zs * A.z);
       };
@@ -433,19 +422,6 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
                 st[5 * 32] = make_float4(-R2s, -R2s, Hc, Hc);
                 st[6 * 32] = make_float4(Hs, Hs, -Hs, -Hs);
                 st[7 * 32] = make_float4(fabsf(dtau), 0.f, 0.f, 0.f);
-                // e^{i omega_0 tau} of this step for every lane of direction dd:
-                // L independent reseeds per lane, off the step loop's critical path
-                {
-                  float2 *row = seeds + ((size_t)dd * 32 + lane) * (L + 1);
-                  const float2 *w0 = sm.w0rev[warp] + dd * L;
-#pragma unroll 4
-                  for (int m = 0; m < L; ++m) {
-                    const float2 w = w0[m];
-                    float zs, zc;
-                    phasor_rev(w.x, w.y, tau.hi, tau.lo, zs, zc);
-                    row[m] = make_float2(zc, zs);
-                  }
-                }
                 const float am = (uint32_t)lane < mcnt ? fabsf(dtau) : 0.f;
                 const float amax =
                     __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(am)));
@@ -591,8 +567,7 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
 }
 
 size_t near_smem_bytes(int dpw) {
-  return sizeof(NearSmemFixed<kNW>) + (size_t)kNW * 32 * dpw * kNSetupF4 * sizeof(float4) +
-         (size_t)kNW * near_seed_f2(dpw) * sizeof(float2);
+  return sizeof(NearSmemFixed<kNW>) + (size_t)kNW * 32 * dpw * kNSetupF4 * sizeof(float4);
 }
 
 template <int K>
