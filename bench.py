@@ -184,27 +184,36 @@ def executed_flops_per_unit(w):
     return 30 if w.args.get("mode", "far") == "near" else FLOPS_PER_UNIT
 
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the
-# dominant kernel in an ncu capture of 16 tracks of the same workload, and the
-# point-steps of that launch.  With the same steps per track the traffic (the
-# per-track partial-spectrum updates and the step records) grows with the
-# number of tracks, as the point-steps do, so a launch's traffic is this
-# ratio times its point-steps.
+# DRAM bytes of one launch of the dominant kernel on the full default
+# workloads, from single-pass ncu captures (dram__bytes_read.sum,
+# dram__bytes_write.sum) of
+#   bench.py --workload W --steps 1 --warmup 1 --no-e2e --no-cpu --no-fp64 --no-graph --shape K L S N
+# with the shape the autotuner picks for that workload.  Most of it is the
+# per-warp compensated sums (written back from L2 on eviction) and the
+# per-subset FP64 partial spectra; neither is on the critical path of these
+# FP32-bound kernels (a few GB/s against ~7 TB/s).
 NCU_TRAFFIC = {
-    "far": (175.7e6 + 212.3e6, 16 * 3999 * 512 * 64 * 64, "far_mixed_kernel<32,8>"),
-    "near": (50.4e6 + 20.3e6, 16 * 7999 * 256 * 64 * 64, "near_mixed_kernel<8>"),
+    # workload: (read bytes, write bytes, tracks, (K, L, stage, subsets), kernel)
+    "far": (1.12e9, 2.72e9, 1024, (32, 16, 64, 10), "far_mixed_kernel<32,8>"),
+    "near": (34.65e9, 260.32e9, 2048, (16, 16, 128, 10), "near_mixed_kernel<16,8>"),
 }
 
 
-def launch_traffic(workload, args, pt_steps):
-    """DRAM bytes per launch scaled from the ncu capture, or None where the
-    capture does not describe this workload (other steps per track or grid)."""
-    if workload not in NCU_TRAFFIC or args.track_steps is not None or args.grid is not None:
+def launch_traffic(workload, args, n_tracks, shape):
+    """DRAM bytes of one launch from the full-size ncu capture, or None where
+    the capture does not describe this run (other tracks, steps or grid)."""
+    if (workload not in NCU_TRAFFIC or args.track_steps is not None or args.grid is not None
+            or args.seed != 0):
         return None, None
-    nbytes, units, src = NCU_TRAFFIC[workload]
-    return (nbytes * pt_steps / units,
-            f"ncu capture of one 16-track launch of {src} (dram__bytes_read.sum + "
-            "dram__bytes_write.sum), scaled by point-steps")
+    rd, wr, nt, sh, src = NCU_TRAFFIC[workload]
+    if n_tracks != nt:
+        return None, None
+    run_sh = (shape["points_per_lane"], shape["lanes_per_direction"],
+              shape["steps_per_stage"], shape["track_subsets"])
+    note = "" if run_sh == sh else f"; this run's shape {run_sh} differs"
+    return (rd + wr,
+            f"ncu capture of one full launch of {src} ({nt} tracks, shape K/L/stage/subsets "
+            f"{sh}): dram__bytes_read.sum {rd:.4g} + dram__bytes_write.sum {wr:.4g}{note}")
 
 
 def product_calc(w):
@@ -640,7 +649,7 @@ def main():
     peak = max(tf_s.value, tf_p.value)
     clk = clocks.summary()
     kname = "near_mixed_kernel" if mode == "near" else "far_mixed_kernel"
-    traffic, traffic_src = launch_traffic(args.workload, args, pt_steps)
+    traffic, traffic_src = launch_traffic(args.workload, args, len(w.tracks), shape)
     roofline = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak if peak else None,
                 "traffic": traffic, "traffic_unit": "bytes per launch",

@@ -1,6 +1,6 @@
 """CPU checks of bench.py's output contract: the reference arm's JSON line
 (it runs the oracle on the host cores, no GPU needed), the silence of ranks
-other than 0 under a multi-rank launch, and the roofline traffic scaling."""
+other than 0 under a multi-rank launch, and the roofline traffic figure."""
 import argparse
 import json
 import os
@@ -50,15 +50,22 @@ def test_reference_arm_other_ranks_print_nothing():
     assert r.stdout.strip() == ""
 
 
-def test_roofline_traffic_scales_with_point_steps():
+def test_roofline_traffic_is_the_full_launch_capture():
+    """The traffic figure is the measured full-size launch, reported only for
+    the run that capture describes (same tracks, steps, grid and seed)."""
     sys.path.insert(0, str(ROOT))
     import bench
-    args = argparse.Namespace(track_steps=None, grid=None)
-    nbytes, units, _ = bench.NCU_TRAFFIC["far"]
-    t1, src = bench.launch_traffic("far", args, units)
-    assert abs(t1 - nbytes) < 1e-6 * nbytes and "ncu" in src
-    t2, _ = bench.launch_traffic("far", args, 64 * units)
-    assert abs(t2 - 64 * nbytes) < 1e-6 * t2
-    assert bench.launch_traffic("ragged", args, units) == (None, None)
-    other = argparse.Namespace(track_steps=100, grid=None)
-    assert bench.launch_traffic("far", other, units) == (None, None)
+    args = argparse.Namespace(track_steps=None, grid=None, seed=0)
+    rd, wr, nt, sh, _ = bench.NCU_TRAFFIC["far"]
+    shape = dict(zip(("points_per_lane", "lanes_per_direction", "steps_per_stage",
+                      "track_subsets"), sh))
+    t, src = bench.launch_traffic("far", args, nt, shape)
+    assert t == rd + wr and "ncu" in src and "differs" not in src
+    other_shape = dict(shape, track_subsets=sh[3] + 1)
+    t, src = bench.launch_traffic("far", args, nt, other_shape)
+    assert t == rd + wr and "differs" in src
+    assert bench.launch_traffic("far", args, nt // 2, shape) == (None, None)
+    assert bench.launch_traffic("ragged", args, nt, shape) == (None, None)
+    for k, v in (("track_steps", 100), ("grid", [8, 8, 8]), ("seed", 3)):
+        other = argparse.Namespace(**dict(vars(args), **{k: v}))
+        assert bench.launch_traffic("far", other, nt, shape) == (None, None)
