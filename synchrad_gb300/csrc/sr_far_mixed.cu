@@ -118,6 +118,22 @@ struct DirConst {
 
 constexpr int kMaxDpw = 4;  // directions per warp (omega tiles narrower than 32 lanes)
 
+// Direction of the warp slot v = (direction group) * dpw + (direction in the
+// warp).  A group holds dpw neighbouring theta at one phi (their masks agree
+// on most steps, so the warp takes the masked path on fewer of them), and
+// the groups run phi first: the W groups of a CTA share their theta range,
+// on which the share of masked steps mostly depends, and wait less for each
+// other at the stage barriers.  Directions are numbered theta first
+// (theta + n_theta * phi); when dpw does not divide n_theta the slots keep
+// that order.
+__device__ __forceinline__ uint32_t dir_of_slot(uint32_t v, uint32_t dpw, uint32_t nT,
+                                                uint32_t nP) {
+  if (nT % dpw != 0u) return v;
+  const uint32_t g = v / dpw;
+  if (g >= (nT / dpw) * nP) return v;
+  return (g / nP) * dpw + v % dpw + nT * (g % nP);
+}
+
 template <int W>
 struct SmemFixed {
   uint64_t bar[2];
@@ -191,7 +207,7 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
     const bool active_w = wt < n_wt;
     const uint32_t dgrp = active_w ? wt / p.n_wtiles : 0u;
     const uint32_t tile = active_w ? wt % p.n_wtiles : 0u;
-    const uint32_t dir_raw = dgrp * dpw + dsub;
+    const uint32_t dir_raw = dir_of_slot(dgrp * dpw + dsub, dpw, nT, p.n_phi);
     const bool active = active_w && dir_raw < n_dirs;
     const uint32_t dir = active ? dir_raw : 0u;
     const int j0 = (int)(tile * (uint32_t)(L * K)) + ll * K;
@@ -389,9 +405,16 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
         if (active_w) {
           for (uint32_t c0 = 0; c0 < cnt; c0 += 32) {
             const uint32_t mcnt = min(32u, cnt - c0);
+            // Classes of the chunk's steps on a uniform axis, one bit per step:
+            // every point of the warp's omega tile included (for all of its
+            // directions), or none possibly included.
+            uint32_t fast_bits = 0u, out_bits = 0u;
             // ---- per-step setup: lane l -> step s0 + c0 + l, every direction ----
             {
               const uint32_t l = (uint32_t)lane < mcnt ? (uint32_t)lane : mcnt - 1;
+              const int tlo = (int)(tile * (uint32_t)(L * K));
+              const int thi = min(tlo + L * K, (int)nO) - 1;
+              bool in_all = true, out_all = true;
               const float4 r0 = stg[(c0 + l) * kRecF4 + 0];
               const float4 r1 = stg[(c0 + l) * kRecF4 + 1];
               const float4 r2 = stg[(c0 + l) * kRecF4 + 2];
@@ -451,6 +474,10 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
                   const float inv_adt = __frcp_rn(fabsf(dtau));
                   omega_interval(w0g, dwg, inv_dwg, kPiLo * inv_adt, (int)nO, jfc, jlc);
                   omega_interval(w0g, dwg, inv_dwg, kPiHi * inv_adt, (int)nO, jfu, jlu);
+                  if (dgrp * dpw + dd < n_dirs) {  // slots map onto [0, n_dirs) one to one
+                    in_all = in_all && jfc <= tlo && jlc >= thi;
+                    out_all = out_all && (jlu < tlo || jfu > thi);
+                  }
                 }
                 st[5 * 32] = make_float4(fabsf(dtau), __int_as_float(jfc), __int_as_float(jlc),
                                          __uint_as_float((uint32_t)jfu | ((uint32_t)(jlu + 1) << 16)));
@@ -462,6 +489,8 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
                 __syncwarp();
                 if (lane == 0) { d.tprev_h = th_last; d.tprev_l = tl_last; d.adt_max = amax; }
               }
+              fast_bits = __ballot_sync(0xffffffffu, iv && (uint32_t)lane < mcnt && in_all);
+              out_bits = __ballot_sync(0xffffffffu, iv && (uint32_t)lane < mcnt && out_all && !in_all);
             }
             __syncwarp();
             // ---- the points: K per lane as two packed rotation chains ----
@@ -514,24 +543,85 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
                 step_seed(st + i, i, zr, zi);
                 step_fast(st + i, zr, zi);
               }
-            } else {
-              // General loop: per-step decision, per-point mask where the
-              // phase advance straddles pi, non-uniform omega, snapshot writes.
+            } else if (iv && __all_sync(0xffffffffu, uniform)) {
+              // Uniform axis: each step's class comes from the setup's ballots
+              // (no per-step vote); a step that is neither fully included nor
+              // fully excluded for the warp keeps, per point, the phasor or a
+              // zero (a select per point: the included points form the index
+              // interval of the setup, widened by the exact FP64 test of the
+              // points inside the guard band).
 #pragma unroll 1
               for (uint32_t i = 0; i < mcnt; ++i) {
                 const float4 *st = setup + (size_t)dsub * 6 * 32 + i;
-                const float4 M = st[5 * 32];
-                const float adt = M.x;
                 const uint32_t s = s0 + c0 + i;
-                const int jfc = __float_as_int(M.y), jlc = __float_as_int(M.z);
-                const uint32_t pu = __float_as_uint(M.w);
-                const int jfu = (int)(pu & 0xffffu), jlu = (int)(pu >> 16) - 1;
-                // a lane is all in (out) when the certain (possible) interval
-                // covers (misses) its points [j0, j0 + nv)
-                const bool all_in = iv ? (jfc <= j0 && jlc >= j0 + nv - 1)
-                                       : (wabs_max * adt < kPiLo);
-                const bool all_out = iv ? (jlu < j0 || jfu > j0 + nv - 1)
-                                        : (wabs_min * adt > kPiHi);
+                if ((fast_bits >> i) & 1u) {
+                  float2 zr, zi;
+                  step_seed(st, i, zr, zi);
+                  step_fast(st, zr, zi);
+                } else if (!((out_bits >> i) & 1u)) {
+                  const float4 M = st[5 * 32];
+                  const int jfc = __float_as_int(M.y), jlc = __float_as_int(M.z);
+                  const uint32_t pu = __float_as_uint(M.w);
+                  const int jfu = (int)(pu & 0xffffu), jlu = (int)(pu >> 16) - 1;
+                  uint32_t mask = range_bits(jfc, jlc, j0, nv);
+                  uint32_t unc = range_bits(jfu, jlu, j0, nv) & ~mask;
+                  if (unc) {
+                    const DirConst &d = sm.dc[warp][dsub];
+                    do {
+                      const int m = __ffs(unc) - 1;
+                      unc &= unc - 1u;
+                      if (exact_mask(p, base, s, it_start, p.omega[j0 + m], d.n0, d.n1, d.cT))
+                        mask |= 1u << m;
+                    } while (unc);
+                  }
+                  float2 ZrA, ZiA;
+                  step_seed(st, i, ZrA, ZiA);
+                  const float4 AT = st[1 * 32], R2 = st[2 * 32], X = st[3 * 32], Y = st[4 * 32];
+                  const float2 at = make_float2(AT.x, AT.y), ap = make_float2(AT.z, AT.w);
+                  const float2 r2c = make_float2(R2.x, R2.y), r2s = make_float2(R2.z, R2.w);
+                  const float2 nr2s = make_float2(X.x, X.y);
+                  float2 ZrB, ZiB;
+                  rot2p(ZrA, ZiA, make_float2(X.z, X.w), make_float2(Y.x, Y.y),
+                        make_float2(Y.z, Y.w), ZrB, ZiB);
+#pragma unroll
+                  for (int q = 0; q < HP; ++q) {
+                    const uint32_t bA = mask >> (2 * q), bB = mask >> (K / 2 + 2 * q);
+                    const float2 mrA = make_float2((bA & 1u) ? ZrA.x : 0.f, (bA & 2u) ? ZrA.y : 0.f);
+                    const float2 miA = make_float2((bA & 1u) ? ZiA.x : 0.f, (bA & 2u) ? ZiA.y : 0.f);
+                    const float2 mrB = make_float2((bB & 1u) ? ZrB.x : 0.f, (bB & 2u) ? ZrB.y : 0.f);
+                    const float2 miB = make_float2((bB & 1u) ? ZiB.x : 0.f, (bB & 2u) ? ZiB.y : 0.f);
+                    aTr[q] = __ffma2_rn(mrA, at, aTr[q]);
+                    aTi[q] = __ffma2_rn(miA, at, aTi[q]);
+                    aPr[q] = __ffma2_rn(mrA, ap, aPr[q]);
+                    aPi[q] = __ffma2_rn(miA, ap, aPi[q]);
+                    aTr[HP + q] = __ffma2_rn(mrB, at, aTr[HP + q]);
+                    aTi[HP + q] = __ffma2_rn(miB, at, aTi[HP + q]);
+                    aPr[HP + q] = __ffma2_rn(mrB, ap, aPr[HP + q]);
+                    aPi[HP + q] = __ffma2_rn(miB, ap, aPi[HP + q]);
+                    if (q + 1 < HP) {
+                      rot2p(ZrA, ZiA, r2c, r2s, nr2s, ZrA, ZiA);
+                      rot2p(ZrB, ZiB, r2c, r2s, nr2s, ZrB, ZiB);
+                    }
+                  }
+                }
+                if ((int64_t)s == snap.fire_it) {  // uniform over the CTA
+                  flush(snap.k);
+                  snap.advance(it_start, it_end, snaps, p.n_snaps);
+                }
+              }
+            } else {
+              // General loop (an omega axis that is not uniform as a whole):
+              // per-step vote, per-lane index interval on uniform lanes and a
+              // per-point test with one reseed per point on the others.
+#pragma unroll 1
+              for (uint32_t i = 0; i < mcnt; ++i) {
+                const float4 *st = setup + (size_t)dsub * 6 * 32 + i;
+                const float adt = st[5 * 32].x;
+                const uint32_t s = s0 + c0 + i;
+                // a lane is all in (out) when its largest (smallest) |omega|
+                // passes (fails) the rule with the guard band
+                const bool all_in = wabs_max * adt < kPiLo;
+                const bool all_out = wabs_min * adt > kPiHi;
                 if (__all_sync(0xffffffffu, uniform && (all_in || nv == 0))) {
                   // every point of the warp included: the straight-line step
                   // (the same products as the masked path with a full mask)
@@ -546,18 +636,13 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
                   uint32_t mask = (all_out || nv == 0) ? 0u : 0xffffffffu;
                   if (!all_in && !all_out && nv > 0) {
                     const DirConst &d = sm.dc[warp][dsub];
-                    if (iv || uniform) {
+                    if (uniform) {
                       // included points form an index interval; only points
                       // inside the guard band need the exact FP64 test
-                      uint32_t unc;
-                      if (iv) {
-                        mask = range_bits(jfc, jlc, j0, nv);
-                        unc = range_bits(jfu, jlu, j0, nv) & ~mask;
-                      } else {
-                        const float inv_adt = __frcp_rn(adt);  // adt > 0 here
-                        mask = omega_range_bits_r(w0f, dwf, inv_dwf, kPiLo * inv_adt, nv);
-                        unc = omega_range_bits_r(w0f, dwf, inv_dwf, kPiHi * inv_adt, nv) & ~mask;
-                      }
+                      const float inv_adt = __frcp_rn(adt);  // adt > 0 here
+                      mask = omega_range_bits_r(w0f, dwf, inv_dwf, kPiLo * inv_adt, nv);
+                      uint32_t unc =
+                          omega_range_bits_r(w0f, dwf, inv_dwf, kPiHi * inv_adt, nv) & ~mask;
                       while (unc) {
                         const int m = __ffs(unc) - 1;
                         unc &= unc - 1u;
@@ -638,6 +723,8 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
             __syncwarp();
           }
           // ---- fold the FP32 sums into the compensated pairs every few stages ----
+          // (all warps at the same stage: a fold staggered by warp made the
+          // other warps wait for it at every stage barrier)
           if ((stage_in_track + 1) % p.fold_stages == 0) fold();
         } else {
           // inactive warp: keep the snapshot state in step with the others
