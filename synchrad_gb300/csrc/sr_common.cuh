@@ -108,22 +108,26 @@ __device__ __forceinline__ df df_mul_raw(df a, df b) {
 
 __device__ __forceinline__ df df_neg(df a) { return df{-a.hi, -a.lo}; }
 __device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
-// sqrt of a positive double-float: float root refined by one Newton step on
-// the exact residual a - x^2 (TwoProduct through FMA).
+// sqrt of a positive double-float: a float root from the hardware reciprocal
+// square root, refined by one Newton step on the exact residual a - x^2
+// (TwoProduct through FMA), which also absorbs the approximate root's error.
 __device__ __forceinline__ df df_sqrt(df a) {
-  const float x = sqrtf(a.hi);
-  if (x == 0.f) return df{0.f, 0.f};
+  if (!(a.hi > 0.f)) return df{0.f, 0.f};
+  const float y = rsqrtf(a.hi);  // ~1/sqrt(a)
+  const float x = a.hi * y;
   const float p = x * x;
   const float e = __fmaf_rn(x, x, -p);
   const float r = ((a.hi - p) - e) + a.lo;
-  return fast_two_sum(x, r * (0.5f / x));
+  return fast_two_sum(x, r * (0.5f * y));
 }
-// a / b for double-floats: quotient, exact remainder, one correction.
+// a / b for double-floats: an approximate quotient, its exact remainder and
+// one correction (the correction absorbs the first quotient's error).
 __device__ __forceinline__ df df_div(df a, df b) {
-  const float q1 = a.hi / b.hi;
+  const float rb = __frcp_rn(b.hi);
+  const float q1 = a.hi * rb;
   const df qb = df_mul(df{q1, 0.f}, b);
   const df r = df_sub(a, qb);
-  const float q2 = (r.hi + r.lo) / b.hi;
+  const float q2 = (r.hi + r.lo) * rb;
   return fast_two_sum(q1, q2);
 }
 

@@ -869,7 +869,7 @@ int launch_far_mixed(FarMixedParams p, const FarMixedConfig &cfg, void *ws, size
   if (cfg.stage < 32 || cfg.stage > 512 || (cfg.stage & 31) != 0)
     return fail(SR_ERR_INVALID, "steps per stage %d (multiples of 32 in [32, 512])", cfg.stage);
   p.stage_steps = (uint32_t)cfg.stage;
-  p.fold_stages = (uint32_t)std::max(1, 1024 / cfg.stage);  // fold about every 1024 steps
+  p.fold_stages = (uint32_t)std::max(1, 2048 / cfg.stage);  // fold about every 2048 steps
 
   cudaError_t e = cudaMemsetAsync(w, 0, 256, stream);
   if (e != cudaSuccess) return cuda_fail(e, "status reset");
