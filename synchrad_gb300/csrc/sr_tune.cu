@@ -204,9 +204,15 @@ extern "C" int sr_autotune(const sr_tracks *t, const sr_grid *g, int comp, int p
   const bool far = g->mode == SR_MODE_FAR;
 
   // Sample: the leading tracks, about budget / 100 ms of work at 2e12 pt-steps/s.
+  // The offsets are read on the call's stream: work queued there before the
+  // call (e.g. the host-to-device copy of a streamed chunk, which the stream
+  // waits for) completes first.  A plain cudaMemcpy runs on the legacy
+  // stream, which does not wait for non-blocking streams, and could read the
+  // buffer before the copy landed.
   std::vector<int64_t> off(t->n_tracks + 1);
-  cudaError_t e = cudaMemcpy(off.data(), t->offsets, off.size() * sizeof(int64_t),
-                             cudaMemcpyDeviceToHost);
+  cudaError_t e = cudaMemcpyAsync(off.data(), t->offsets, off.size() * sizeof(int64_t),
+                                  cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "offsets read");
   const double target = std::max(1e9, budget_ms / 100.0 * 2e9);
   uint32_t n_s = 1;
