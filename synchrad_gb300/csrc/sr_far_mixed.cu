@@ -23,7 +23,7 @@
 //  * the |dphase| < pi mask is decided per step from |omega| |dtau| with a
 //    guard band; inside the band the reference's FP64 expression is evaluated
 //    bit for bit from the original track data.
-//  * sums are FP32 for 1024 steps at a time and then folded into compensated
+//  * sums are FP32 for 2048 steps at a time and then folded into compensated
 //    (Knuth TwoSum) FP32 pairs kept in an L2-resident workspace; per-track
 //    results are formed and accumulated in FP64.
 //
@@ -140,6 +140,7 @@ struct SmemFixed {
   uint32_t next_item;   // broadcast of the work item taken from the queue
   uint32_t pad32_;
   uint64_t pad_[1];
+  float2 gate[4];       // gate[b] = (b & 1, b >> 1): a point pair's mask bits as factors
   DirConst dc[W][kMaxDpw];
   // followed by float4 setup[W][dpw][6][32], then the two stage buffers of
   // p.stage_steps step records each
@@ -168,6 +169,8 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
     mbar_init(&sm.bar[1], 1);
     fence_mbar_init();
   }
+  if (threadIdx.x < 4)
+    sm.gate[threadIdx.x] = make_float2((float)(threadIdx.x & 1u), (float)(threadIdx.x >> 1));
   __syncthreads();
 
   const uint32_t nO = p.n_omega, nT = p.n_theta;
@@ -585,11 +588,12 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
                         make_float2(Y.z, Y.w), ZrB, ZiB);
 #pragma unroll
                   for (int q = 0; q < HP; ++q) {
-                    const uint32_t bA = mask >> (2 * q), bB = mask >> (K / 2 + 2 * q);
-                    const float2 mrA = make_float2((bA & 1u) ? ZrA.x : 0.f, (bA & 2u) ? ZrA.y : 0.f);
-                    const float2 miA = make_float2((bA & 1u) ? ZiA.x : 0.f, (bA & 2u) ? ZiA.y : 0.f);
-                    const float2 mrB = make_float2((bB & 1u) ? ZrB.x : 0.f, (bB & 2u) ? ZrB.y : 0.f);
-                    const float2 miB = make_float2((bB & 1u) ? ZiB.x : 0.f, (bB & 2u) ? ZiB.y : 0.f);
+                    // the pair's two mask bits pick its 0/1 factors from a
+                    // 4-entry table (one shared load, no per-point selects)
+                    const float2 gA = sm.gate[(mask >> (2 * q)) & 3u];
+                    const float2 gB = sm.gate[(mask >> (K / 2 + 2 * q)) & 3u];
+                    const float2 mrA = __fmul2_rn(ZrA, gA), miA = __fmul2_rn(ZiA, gA);
+                    const float2 mrB = __fmul2_rn(ZrB, gB), miB = __fmul2_rn(ZiB, gB);
                     aTr[q] = __ffma2_rn(mrA, at, aTr[q]);
                     aTi[q] = __ffma2_rn(miA, at, aTi[q]);
                     aPr[q] = __ffma2_rn(mrA, ap, aPr[q]);
