@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
   const uint32_t n_groups_dir = (n_dirs + dpw - 1) / dpw;  // direction groups
   const uint32_t n_wt = n_groups_dir * p.n_wtiles;         // warp tasks
   const double dw_glob = (nO > 1) ? (p.omega[nO - 1] - p.omega[0]) / (double)(nO - 1) : 0.0;
-  const df d_dw = df_from_double(dw_glob);
+  const df d_dw_rev = df_from_double(dw_glob * 0.15915494309189533577);  // d_omega / 2 pi
   const double inv2pi = 0.15915494309189533577;
   float *outer = p.outer + ((size_t)blockIdx.x * W + warp) * K * 8 * 32;
   uint32_t stage_no = 0;  // running stage counter (mbarrier phase bookkeeping)
@@ -451,10 +451,9 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
                 const float amp_p = -(c1 * pb + c2 * pa);
                 // rotation between neighbouring omega points, its square, and
                 // its power K/2 (start of the second chain)
-                const df rp = df_mul_raw(d_dw, tau);
-                const float rr = reduce_2pi(rp.hi, rp.lo);
+                const df rp = df_mul_raw(d_dw_rev, tau);  // revolutions
                 float Rs, Rc;
-                sincosf(rr, &Rs, &Rc);
+                cis_rev(rp.hi, rp.lo, Rs, Rc);
                 float R2c, R2s;
                 cmul(Rc, Rs, Rc, Rs, R2c, R2s);
                 float Hc = 1.f, Hs = 0.f, Pc = Rc, Ps = Rs;
@@ -536,10 +535,10 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
                 }
               }
             };
-            // warp-uniform choice: the whole warp runs the tight loop or the
-            // general one (lanes of a warp never diverge between the two)
+            // warp-uniform choices (lanes of a warp never diverge between paths)
             if (__all_sync(0xffffffffu, uniform && !fire_here &&
                            wabs_max * sm.dc[warp][dsub].adt_max < kPiLo)) {
+              // every step of the chunk included for every point: the tight loop
               const float4 *st = setup + (size_t)dsub * 6 * 32;
               for (uint32_t i = 0; i < mcnt; ++i) {
                 float2 zr, zi;
@@ -548,20 +547,30 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
               }
             } else if (iv && __all_sync(0xffffffffu, uniform)) {
               // Uniform axis: each step's class comes from the setup's ballots
-              // (no per-step vote); a step that is neither fully included nor
-              // fully excluded for the warp keeps, per point, the phasor or a
-              // zero (a select per point: the included points form the index
+              // (no per-step vote). Runs of included steps go through the
+              // straight-line loop; a step that is neither fully included nor
+              // fully excluded for the warp takes the masked step (its points'
+              // phasors times 0/1 factors: the included points form the index
               // interval of the setup, widened by the exact FP64 test of the
-              // points inside the guard band).
+              // points inside the guard band). In a chunk with a snapshot write
+              // every step takes the per-step path, which checks for the write
+              // after each step (an included step there is a masked step with a
+              // full mask).
+              const float4 *stb = setup + (size_t)dsub * 6 * 32;
+              const uint32_t fb = fire_here ? 0u : fast_bits;
+              uint32_t i = 0;
 #pragma unroll 1
-              for (uint32_t i = 0; i < mcnt; ++i) {
-                const float4 *st = setup + (size_t)dsub * 6 * 32 + i;
-                const uint32_t s = s0 + c0 + i;
-                if ((fast_bits >> i) & 1u) {
+              while (i < mcnt) {
+                const uint32_t run = min((uint32_t)__ffs(~(fb >> i)) - 1u, mcnt - i);
+                for (const uint32_t e = i + run; i < e; ++i) {
                   float2 zr, zi;
-                  step_seed(st, i, zr, zi);
-                  step_fast(st, zr, zi);
-                } else if (!((out_bits >> i) & 1u)) {
+                  step_seed(stb + i, i, zr, zi);
+                  step_fast(stb + i, zr, zi);
+                }
+                if (i >= mcnt) break;
+                const float4 *st = stb + i;
+                const uint32_t s = s0 + c0 + i;
+                if (!((out_bits >> i) & 1u)) {
                   const float4 M = st[5 * 32];
                   const int jfc = __float_as_int(M.y), jlc = __float_as_int(M.z);
                   const uint32_t pu = __float_as_uint(M.w);
@@ -612,6 +621,7 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
                   flush(snap.k);
                   snap.advance(it_start, it_end, snaps, p.n_snaps);
                 }
+                ++i;
               }
             } else {
               // General loop (an omega axis that is not uniform as a whole):
