@@ -9,7 +9,7 @@ namespace {
 
 constexpr int kStage = 128;         // steps per TMA stage
 constexpr size_t kMaxSmemPerCta = 232448;  // opt-in shared memory per CTA (227 KB)
-constexpr int kFoldStages = 16;     // FP32 sums fold into compensated pairs every 2048 steps
+constexpr int kFoldStages = 32;     // near field: FP32 sums fold into compensated pairs every 4096 steps
 // float4 per step record: 64 bytes of data and 16 of padding, so that 32
 // lanes reading one record each from shared memory hit every bank once per
 // quarter warp (at a 64-byte stride four lanes in eight share the same banks)
