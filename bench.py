@@ -191,11 +191,11 @@ def executed_flops_per_unit(w):
 # with the shape the autotuner picks for that workload.  Most of it is the
 # per-warp compensated sums (written back from L2 on eviction) and the
 # per-subset FP64 partial spectra; neither is on the critical path of these
-# FP32-bound kernels (2-19 GB/s against ~7 TB/s).
+# FP32-bound kernels (2-14 GB/s against ~7 TB/s).
 NCU_TRAFFIC = {
     # workload: (read bytes, write bytes, tracks, (K, L, stage, subsets), kernel)
     "far": (1.12e9, 5.01e9, 1024, (32, 16, 64, 10), "far_mixed_kernel<32,8>"),
-    "near": (18.53e9, 191.46e9, 2048, (16, 16, 128, 10), "near_mixed_kernel<16,8>"),
+    "near": (5.97e9, 142.33e9, 2048, (16, 16, 128, 10), "near_mixed_kernel<16,8>"),
 }
 
 
