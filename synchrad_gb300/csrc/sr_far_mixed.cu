@@ -456,11 +456,18 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
                 cis_rev(rp.hi, rp.lo, Rs, Rc);
                 float R2c, R2s;
                 cmul(Rc, Rs, Rc, Rs, R2c, R2s);
-                float Hc = 1.f, Hs = 0.f, Pc = Rc, Ps = Rs;
+                // H = R^(K/2) = (R^2)^(K/4) by binary powering from R^2 (the
+                // exponent is a compile-time constant: K = 32 takes three
+                // squarings, K = 24 two squarings and one product)
+                float Hc = R2c, Hs = R2s, Pc = R2c, Ps = R2s;
+                bool h_set = false;
 #pragma unroll
-                for (int e = K / 2; e > 0; e >>= 1) {
-                  if (e & 1) cmul(Hc, Hs, Pc, Ps, Hc, Hs);
-                  cmul(Pc, Ps, Pc, Ps, Pc, Ps);
+                for (int e = K / 4; e > 0; e >>= 1) {
+                  if (e & 1) {
+                    if (h_set) cmul(Hc, Hs, Pc, Ps, Hc, Hs);
+                    else { Hc = Pc; Hs = Ps; h_set = true; }
+                  }
+                  if (e > 1) cmul(Pc, Ps, Pc, Ps, Pc, Ps);
                 }
                 // setup[dd][k][step]: consecutive lanes store consecutive float4
                 float4 *st = setup + (size_t)dd * 6 * 32 + lane;
