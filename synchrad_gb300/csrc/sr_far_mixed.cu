@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
   const uint32_t n_groups_dir = (n_dirs + dpw - 1) / dpw;  // direction groups
   const uint32_t n_wt = n_groups_dir * p.n_wtiles;         // warp tasks
   const double dw_glob = (nO > 1) ? (p.omega[nO - 1] - p.omega[0]) / (double)(nO - 1) : 0.0;
-  const df d_dw_rev = df_from_double(dw_glob * 0.15915494309189533577);  // d_omega / 2 pi
+  const df d_dw = df_from_double(dw_glob);
   const double inv2pi = 0.15915494309189533577;
   float *outer = p.outer + ((size_t)blockIdx.x * W + warp) * K * 8 * 32;
   uint32_t stage_no = 0;  // running stage counter (mbarrier phase bookkeeping)
@@ -451,9 +451,10 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
                 const float amp_p = -(c1 * pb + c2 * pa);
                 // rotation between neighbouring omega points, its square, and
                 // its power K/2 (start of the second chain)
-                const df rp = df_mul_raw(d_dw_rev, tau);  // revolutions
+                const df rp = df_mul_raw(d_dw, tau);
+                const float rr = reduce_2pi(rp.hi, rp.lo);
                 float Rs, Rc;
-                cis_rev(rp.hi, rp.lo, Rs, Rc);
+                sincosf(rr, &Rs, &Rc);
                 float R2c, R2s;
                 cmul(Rc, Rs, Rc, Rs, R2c, R2s);
                 // H = R^(K/2) = (R^2)^(K/4) by binary powering from R^2 (the

@@ -61,16 +61,6 @@ __device__ __forceinline__ void phasor_rev(float wh, float wl, float th, float t
   __sincosf(f * 6.28318530717958648f, &s, &c);
 }
 
-// sin and cos of 2 pi p for a double-float p in revolutions (the rotation
-// between neighbouring omega points): whole turns dropped exactly, the
-// fraction in [-1/2, 1/2] to sincospif, whose argument needs no further
-// reduction.
-__device__ __forceinline__ void cis_rev(float hi, float lo, float &s, float &c) {
-  const float n = rintf(hi);
-  const float f = (hi - n) + lo;
-  sincospif(2.f * f, &s, &c);
-}
-
 // The reference's mask test evaluated exactly as the FP64 kernel does it
 // (synchrad/kernel_farfield.cl:65-72), for one point and step.
 __device__ __noinline__ bool exact_mask(const FarMixedParams &p, int64_t base, uint32_t s,

@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
   const uint32_t n_groups_dir = (n_dirs + dpw - 1) / dpw;
   const uint32_t n_wt = n_groups_dir * p.n_wtiles;
   const double dw_glob = (nO > 1) ? (p.omega[nO - 1] - p.omega[0]) / (double)(nO - 1) : 0.0;
-  const df d_dw_rev = df_from_double(dw_glob * 0.15915494309189533577);  // d_omega / 2 pi
+  const df d_dw = df_from_double(dw_glob);
   const df dL = df_from_double(p.L_screen);
   const double inv2pi = 0.15915494309189533577;
   float *outer = p.outer + ((size_t)blockIdx.x * W + warp) * K * kNOuter * 32;
@@ -404,9 +404,9 @@ __global__ void __launch_bounds__(W * 32, 1) near_mixed_kernel(FarMixedParams p)
                 const float bz = (omn - r2.w) * rinv;
                 const float rr = rinv * rinv;
                 const float ax = nx * rr, ay = ny * rr, az = nz * rr;
-                const df rp = df_mul_raw(d_dw_rev, tau);  // revolutions
+                const df rp = df_mul_raw(d_dw, tau);
                 float Rs, Rc;
-                cis_rev(rp.hi, rp.lo, Rs, Rc);
+                sincosf(reduce_2pi(rp.hi, rp.lo), &Rs, &Rc);
                 float R2c, R2s;
                 cmul(Rc, Rs, Rc, Rs, R2c, R2s);
                 float Hc = R2c, Hs = R2s;  // R^(K/2) by squaring R^2
