@@ -188,6 +188,8 @@ typedef struct sr_config {
  * size after tuning).  Allocates and frees its own scratch; stops starting new
  * candidates once budget_ms (<= 0: 3000) has passed.  best / dflt (either may
  * be NULL) receive the chosen and the default shape with their sample times.
+ * Runs on `stream` and synchronises it: the track arrays may still be
+ * arriving by copies that `stream` waits for (the offsets are read on it).
  * SR_PREC_MIXED only. */
 int sr_autotune(const sr_tracks *tracks, const sr_grid *grid, int comp, int precision,
                 double budget_ms, void *stream, sr_config *best, sr_config *dflt);
