@@ -117,6 +117,10 @@ struct DirConst {
 };
 
 constexpr int kMaxDpw = 4;  // directions per warp (omega tiles narrower than 32 lanes)
+// float4 per direction in a warp's setup block: 6 values x 32 steps, plus one
+// so that the blocks of two directions read by the same 16-lane half-warp
+// (4 directions per warp) start in different 16-byte bank groups
+constexpr int kSetupStride = 6 * 32 + 1;
 
 // Direction of the warp slot v = (direction group) * dpw + (direction in the
 // warp).  A group holds dpw neighbouring theta at one phi (their masks agree
@@ -142,7 +146,7 @@ struct SmemFixed {
   uint64_t pad_[1];
   float2 gate[4];       // gate[b] = (b & 1, b >> 1): a point pair's mask bits as factors
   DirConst dc[W][kMaxDpw];
-  // followed by float4 setup[W][dpw][6][32], then the two stage buffers of
+  // followed by float4 setup[W][dpw][kSetupStride] ([6][32] used), then the two stage buffers of
   // p.stage_steps step records each
 };
 
@@ -157,10 +161,10 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
   float4 *setup_all = reinterpret_cast<float4 *>(smem_raw + sizeof(SmemFixed<W>));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int dsub = lane / L, ll = lane % L;
-  float4 *setup = setup_all + (size_t)warp * 32 * dpw * 6;
+  float4 *setup = setup_all + (size_t)warp * dpw * kSetupStride;
   const uint32_t S = p.stage_steps;  // steps per TMA stage
   float4 *stage_buf[2];
-  stage_buf[0] = setup_all + (size_t)W * 32 * dpw * 6;
+  stage_buf[0] = setup_all + (size_t)W * dpw * kSetupStride;
   stage_buf[1] = stage_buf[0] + (size_t)S * kRecF4;
   constexpr int KP = K / 2, HP = KP / 2;
 
@@ -471,7 +475,7 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
                   if (e > 1) cmul(Pc, Ps, Pc, Ps, Pc, Ps);
                 }
                 // setup[dd][k][step]: consecutive lanes store consecutive float4
-                float4 *st = setup + (size_t)dd * 6 * 32 + lane;
+                float4 *st = setup + (size_t)dd * kSetupStride + lane;
                 st[0 * 32] = make_float4(tau.hi, tau.lo, Rc, Rs);
                 st[1 * 32] = make_float4(amp_t, amp_t, amp_p, amp_p);
                 st[2 * 32] = make_float4(R2c, R2c, R2s, R2s);
@@ -547,7 +551,7 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
             if (__all_sync(0xffffffffu, uniform && !fire_here &&
                            wabs_max * sm.dc[warp][dsub].adt_max < kPiLo)) {
               // every step of the chunk included for every point: the tight loop
-              const float4 *st = setup + (size_t)dsub * 6 * 32;
+              const float4 *st = setup + (size_t)dsub * kSetupStride;
               for (uint32_t i = 0; i < mcnt; ++i) {
                 float2 zr, zi;
                 step_seed(st + i, i, zr, zi);
@@ -564,7 +568,7 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
               // every step takes the per-step path, which checks for the write
               // after each step (an included step there is a masked step with a
               // full mask).
-              const float4 *stb = setup + (size_t)dsub * 6 * 32;
+              const float4 *stb = setup + (size_t)dsub * kSetupStride;
               const uint32_t fb = fire_here ? 0u : fast_bits;
               uint32_t i = 0;
 #pragma unroll 1
@@ -637,7 +641,7 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
               // per-point test with one reseed per point on the others.
 #pragma unroll 1
               for (uint32_t i = 0; i < mcnt; ++i) {
-                const float4 *st = setup + (size_t)dsub * 6 * 32 + i;
+                const float4 *st = setup + (size_t)dsub * kSetupStride + i;
                 const float adt = st[5 * 32].x;
                 const uint32_t s = s0 + c0 + i;
                 // a lane is all in (out) when its largest (smallest) |omega|
@@ -774,7 +778,7 @@ __global__ void __launch_bounds__(W * 32, 1) far_mixed_kernel(FarMixedParams p) 
 constexpr int kW = 8;  // warps per CTA
 
 size_t smem_bytes(int dpw, int stage) {
-  return sizeof(SmemFixed<kW>) + (size_t)kW * 32 * dpw * 6 * sizeof(float4) +
+  return sizeof(SmemFixed<kW>) + (size_t)kW * dpw * kSetupStride * sizeof(float4) +
          (size_t)2 * stage * kRecF4 * sizeof(float4);
 }
 
