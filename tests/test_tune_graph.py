@@ -101,7 +101,7 @@ def test_autotune_choice_is_used_and_accurate(mode):
 @pytest.mark.parametrize("stage", [32, 64, 256, 512])
 def test_far_stage_sizes_agree(stage):
     """Every steps-per-stage a pinned or tuned shape may use gives the same
-    spectrum to rounding (the fold interval stays about 1024 steps)."""
+    spectrum to rounding (the fold interval stays about 2048 steps)."""
     _need_gpu()
     from synchrad_gb300 import _lib
     from synchrad_gb300 import batch as bt
@@ -112,6 +112,39 @@ def test_far_stage_sizes_agree(stage):
     bt.set_config(batch, grid, points_per_lane=16, lanes_per_direction=16, steps_per_stage=stage)
     used = bt.current_config(batch, grid)
     assert used["steps_per_stage"] == stage and used["points_per_lane"] == 16
+    got = _spectrum(batch, grid, n, _lib.SR_PREC_MIXED)
+    _lib.lib().sr_config_clear()
+    assert _rel(got, ref) <= TOL_MIXED
+
+
+@pytest.mark.parametrize("K", [16, 32])
+@pytest.mark.parametrize("L", [8, 16, 32])
+@pytest.mark.parametrize("n_theta", [7, 12])
+@pytest.mark.parametrize("case", ["included", "masked"])
+def test_far_shapes_agree(K, L, n_theta, case):
+    """The far-field kernel at every lane count (1, 2 or 4 directions per
+    warp) stays within the mixed tolerance of the FP64 kernel: 12 theta nodes
+    take the theta-group direction order (groups of 32/L neighbouring theta,
+    phi first), 7 the plain order; 5 phi nodes leave the last CTA's groups
+    partial; 70 omega points are no multiple of the lane tile.  "masked"
+    starts the axis at 0 on coarse tracks, so the |dphase| < pi mask cuts
+    through the tile on most steps (setup ballots, masked and skipped steps,
+    runs of included steps)."""
+    _need_gpu()
+    from synchrad_gb300 import _lib
+    from synchrad_gb300 import batch as bt
+    w = wl.c2_far_mixed(n_tracks=6, n_steps=800 if case == "included" else 150,
+                        grid=(70, n_theta, 5))
+    if case == "masked":
+        g = list(w.args["grid"])
+        g[0] = (0.0, g[0][1])
+        w.args["grid"] = g
+    batch, grid, n = _setup(w)
+    ref = _spectrum(batch, grid, n, _lib.SR_PREC_DOUBLE)
+    _lib.lib().sr_config_clear()
+    bt.set_config(batch, grid, points_per_lane=K, lanes_per_direction=L, steps_per_stage=64)
+    used = bt.current_config(batch, grid)
+    assert used["points_per_lane"] == K and used["lanes_per_direction"] == L
     got = _spectrum(batch, grid, n, _lib.SR_PREC_MIXED)
     _lib.lib().sr_config_clear()
     assert _rel(got, ref) <= TOL_MIXED
